@@ -1,0 +1,316 @@
+"""Throughput benchmark of the GB300 synthesis engine.
+
+Workload (one "step"): the render-texture enlarge -- a 128x128 RGBA corpus tile
+of seeded value noise plus tileable stripes synthesized into a 1024x1024
+target, random order, neighbours=16, trys=300, no context -- through
+engine() (wavefront mode), all passes until the reference's termination rule.
+
+  value   target px/s with the pixmaps already resident in device memory
+          (engineDevice), timed with CUDA events per step, L2 flushed between
+          steps (outside the timed intervals)
+  e2e     the same metric through engineEx() with host Maps: host->device copy
+          of the pixmaps, the synthesis and the device->host copy of the result
+  roofline    the per-target synthesis kernel (k_wave), its launches timed live
+          with CUDA events on the library stream
+  cpu_baseline  the CPU engine on a bounded sample of the workload
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "render1024: 128x128 RGBA tile -> 1024x1024 target, random order, P=16, trys=300, engine()"
+METRIC = "target px/s + candidate evals/s; learned vs plain GPU search at equal patch energy"
+TERM_BYTES = 4 + 2 * 3            # corpus word (mask + RGB) + three 16-bit table reads per neighbour term
+TERM_OPS = 4 + 3 * 3              # bounds/mask + (sub, index, add) per colour channel
+SAMPLE_SIDE = 256                 # CPU sample: 256x256 target from the same tile
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(threads: int, side: int = SAMPLE_SIDE):
+    """The CPU engine on a side x side sample of the workload: the reference
+    built from its own sources where present, else the oracle port."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from resynthesizer_gb300 import workloads as W
+    wl = W.render(tile=128, out=side)
+    p = O.make_params(**wl["params"])
+    kind = "port"
+    if O.reference_available(threaded=threads > 1):
+        ref = O.Reference(threaded=threads > 1)
+        fmt = O.Oracle().format_indices(*wl["format"])
+        t0 = time.perf_counter()
+        rc, _, _, _ = ref.engine_state(p, fmt, wl["target"], wl["corpus"])
+        dt = time.perf_counter() - t0
+        kind = "reference"
+        evals = None
+    else:
+        o = O.Oracle()
+        fmt = o.format_indices(*wl["format"])
+        t0 = time.perf_counter()
+        rc, _, st = o.engine(p, fmt, wl["target"], wl["corpus"], threads=threads)
+        dt = time.perf_counter() - t0
+        evals = st.evals
+    assert rc == 0
+    px = side * side
+    return dict(value=px / dt, seconds=dt, evals_per_s=(evals / dt) if evals else None, kind=kind, cores=threads,
+                sample=f"{side}x{side} target from the same 128x128 tile (P=16, trys=300), one run")
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    # The reference's threaded engine (THREAD_LIMIT = 8 worker threads,
+    # lib/buildSwitches.h:89) on a bounded sample per step.
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(threads=8)
+        if i >= args.warmup:
+            vals.append(r)
+    total_px = SAMPLE_SIDE * SAMPLE_SIDE * len(vals)
+    total_s = sum(v["seconds"] for v in vals)
+    value = total_px / total_s
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "target px/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / len(vals),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": vals[0]["sample"], "threads": 8},
+            "cpu_baseline": {"value": value, "unit": "target px/s", "cores": 8, "kind": vals[0]["kind"],
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": value, "unit": "target px/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--out", type=int, default=1024)
+    ap.add_argument("--profile-once", action="store_true",
+                    help="one warm-up and one timed engineDevice call only (for ncu captures)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import numpy as np
+    import torch
+
+    import resynthesizer_gb300 as R
+    from resynthesizer_gb300 import build as B
+    from resynthesizer_gb300 import workloads as W
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if rank == 0 or world == 1:
+        B.build()
+    if world > 1:
+        dist.barrier()
+    L = R.lib()
+
+    wl = W.render(tile=128, out=args.out)
+    p = R.params(**wl["params"])
+    fmt = R.format_indices(*wl["format"])
+    th, tw, _ = wl["target"].shape
+    ch, cw, _ = wl["corpus"].shape
+    dev = torch.device("cuda", local)
+    t_init = torch.from_numpy(wl["target"]).to(dev)
+    t_work = t_init.clone()
+    c_dev = torch.from_numpy(wl["corpus"]).to(dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    opts = R.options(mode=R.MODE_WAVEFRONT)
+
+    def step(o=opts):
+        t_work.copy_(t_init)
+        rc, st = R.engine_device(p, fmt, t_work.data_ptr(), tw, th, c_dev.data_ptr(), cw, ch,
+                                 stream=stream.cuda_stream, opts=o)
+        if rc:
+            raise RuntimeError(f"engineDevice rc={rc}: {R.last_error()}")
+        return st
+
+    if args.profile_once:
+        step()
+        torch.cuda.synchronize()
+        st = step()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_once": True, "stats": st}), flush=True)
+        return
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+
+    # device-resident throughput
+    ms, evals, launches = [], 0, 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            evals += st["evals"]
+            launches += st["launches"]
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    value = world * args.steps * tw * th / (total_ms / 1000.0)
+    evals_per_s = world * evals / (total_ms / 1000.0)
+
+    # end to end through the reference-facing call with host buffers
+    e2e_ms, h2d, d2h = [], 0, 0
+    for i in range(args.warmup + args.steps):
+        tm, cm = R.PixmapMap(wl["target"]), R.PixmapMap(wl["corpus"])
+        stt = R.Stats()
+        t0 = time.perf_counter()
+        rc = L.engineEx(R.C.byref(p), R.C.byref(fmt), R.C.byref(tm.map), R.C.byref(cm.map), None, None, None,
+                        R.C.byref(opts), R.C.byref(stt))
+        dt = time.perf_counter() - t0
+        assert rc == 0, R.last_error()
+        if i >= args.warmup:
+            e2e_ms.append(dt * 1000)
+            h2d, d2h = stt.h2dBytes, stt.d2hBytes
+    e2e_value = world * args.steps * tw * th / (sum(e2e_ms) / 1000.0)
+
+    # dominant kernel: the per-target synthesis launches, timed live
+    flush.fill_(1)
+    torch.cuda.synchronize()
+    prof = step(R.options(mode=R.MODE_WAVEFRONT, profile=1))
+    wave_ms_per_launch = prof["waveMs"] / max(1, prof["waveLaunches"])
+    terms_per_launch = prof["waveTerms"] / max(1, prof["waveLaunches"])
+    achieved_gbs = terms_per_launch * TERM_BYTES / (wave_ms_per_launch / 1000.0) / 1e9
+    peak, peak_kind = peaks()
+
+    # quality of this run (outside every timed region)
+    res = R.engine(wl["target"], wl["corpus"], fmt, p, opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1))
+    sel = wl["target"][..., 0] != 0
+    ys, xs = np.nonzero(sel)
+    targets = np.stack([xs, ys], 1).astype(np.int32)
+    energy, _ = R.patch_energy(p, fmt, res.out, wl["corpus"], res.has_value, res.source, targets)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "target px/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "target": f"{tw}x{th}", "corpus": f"{cw}x{ch}", "mode": "wavefront",
+                   "l2": "flushed (256 MB write) between steps, outside the timed intervals",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "evals_per_s": evals_per_s,
+        "energy_per_px": energy / (tw * th),
+        "passes": res.stats["passes"],
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": "target px/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": achieved_gbs / peak, "traffic": None, "kernel": "k_wave",
+                     "peak_kind": peak_kind, "launches": prof["waveLaunches"],
+                     "ms_per_launch": wave_ms_per_launch, "terms_per_launch": terms_per_launch,
+                     "bytes_per_term": TERM_BYTES, "int_ops_per_s": terms_per_launch * TERM_OPS /
+                     (wave_ms_per_launch / 1000.0)},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        mt = cpu_sample(threads=8)
+        stt = cpu_sample(threads=1)
+        line["cpu_baseline"] = {"value": mt["value"], "unit": "target px/s", "cores": 8, "kind": mt["kind"],
+                                "sample": mt["sample"], "single_thread_value": stt["value"]}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

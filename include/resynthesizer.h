@@ -1,0 +1,234 @@
+/*
+ * resynthesizer.h -- C ABI of the GB300 synthesis engine (libresynthesizer.so).
+ *
+ * Drop-in for the reference's library interface: a caller compiled against
+ * the reference headers (lib/imageSynth.h, lib/engine.h, lib/map.h,
+ * lib/engineParams.h, lib/imageFormatIndicies.h) links against this library
+ * unchanged.  Every declaration below states the reference declaration it
+ * replaces; types keep the reference's memory layout.  Work runs on the
+ * current CUDA device; there is no CPU fallback -- without a usable GPU the
+ * synthesis entry points return RESYNTH_ERROR_DEVICE.
+ */
+#ifndef RESYNTHESIZER_GB300_H
+#define RESYNTHESIZER_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ types */
+
+/* lib/imageBuffer.h:12-19 */
+typedef struct _ImageBuffer {
+  unsigned char *data;
+  unsigned int width;
+  unsigned int height;
+  size_t rowBytes;
+} ImageBuffer;
+
+/* lib/imageFormat.h:36-42 */
+typedef enum ImageFormat { T_RGB, T_RGBA, T_Gray, T_GrayA } TImageFormat;
+
+/* lib/engineParams.h:13-28, plus codes of this library from 100 on. */
+typedef enum ImageSynthError {
+  IMAGE_SYNTH_SUCCESS,
+  IMAGE_SYNTH_ERROR_INVALID_IMAGE_FORMAT,
+  IMAGE_SYNTH_ERROR_IMAGE_MASK_MISMATCH,
+  IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED,
+  IMAGE_SYNTH_ERROR_MATCH_CONTEXT_TYPE_RANGE,
+  IMAGE_SYNTH_ERROR_EMPTY_TARGET,
+  IMAGE_SYNTH_ERROR_EMPTY_CORPUS,
+  RESYNTH_ERROR_DEVICE = 100,        /* CUDA unavailable or a CUDA call failed */
+  RESYNTH_ERROR_UNSUPPORTED = 101,   /* pixel layout or size outside the engine's limits */
+  RESYNTH_ERROR_ARGUMENT = 102       /* NULL or inconsistent argument to an extension call */
+} TImageSynthError;
+
+/* lib/engineParams.h:31-86 */
+typedef struct ImageSynthParametersStruct {
+  int isMakeSeamlesslyTileableHorizontally;
+  int isMakeSeamlesslyTileableVertically;
+  int matchContextType;
+  double mapWeight;
+  double sensitivityToOutliers;
+  unsigned int patchSize;
+  unsigned int maxProbeCount;
+} TImageSynthParameters;
+
+/* lib/imageFormatIndicies.h:39-58 */
+typedef unsigned char TPixelelIndex;
+typedef struct indicesStruct {
+  TPixelelIndex colorEndBip;
+  TPixelelIndex alpha_bip;
+  TPixelelIndex map_start_bip;
+  TPixelelIndex map_end_bip;
+  TPixelelIndex img_match_bpp;
+  TPixelelIndex map_match_bpp;
+  TPixelelIndex total_bpp;
+  int isAlphaTarget;
+  int isAlphaSource;
+} TFormatIndices;
+
+/* lib/glibProxy.h:86-92 (same layout as GLib's public GArray). */
+typedef struct _GArray {
+  char *data;
+  unsigned int len;
+} GArray;
+
+/* lib/map.h:28-46 */
+typedef struct {
+  unsigned int width;
+  unsigned int height;
+  unsigned int depth;
+  GArray *data;
+} Map;
+typedef unsigned char Pixelel;
+typedef struct { int x; int y; } Coordinates;
+
+/* ------------------------------------------------- reference entry points */
+
+/* lib/imageSynth.h:31-40 (def lib/imageSynth.c:61-137) */
+int imageSynth(ImageBuffer *imageBuffer, ImageBuffer *mask, TImageFormat imageFormat,
+               TImageSynthParameters *parameters, void (*progressCallback)(int, void *),
+               void *contextInfo, int *cancelFlag);
+
+/* lib/imageSynth.h:42-52 (def lib/imageSynth.c:139-216) */
+int imageSynth2(ImageBuffer *imageBuffer, ImageBuffer *mask, ImageBuffer *mask2,
+                TImageFormat imageFormat, TImageSynthParameters *parameters,
+                void (*progressCallback)(int, void *), void *contextInfo, int *cancelFlag);
+
+/* lib/engine.h:3-12 (def lib/engine.c:539-690) */
+int engine(TImageSynthParameters parameters, TFormatIndices *indices, Map *targetMap, Map *corpusMap,
+           void (*progressCallback)(int, void *), void *contextInfo, int *cancelFlag);
+
+/* lib/engineParams.h:91-94 (def lib/engineParams.c:8-19) */
+void setDefaultParams(TImageSynthParameters *param);
+
+/* lib/imageFormatIndicies.h:60-84 (defs lib/imageFormat.c:39-241) */
+unsigned int countPixelelsPerPixelForFormat(TImageFormat format);
+int prepareImageFormatIndicesFromFormatType(TFormatIndices *indices, TImageFormat format);
+void prepareImageFormatIndices(TFormatIndices *indices, unsigned int count_color_channels_target,
+                               unsigned int count_color_channels_map, int is_alpha_target,
+                               int is_alpha_source, int isMap);
+void prepareDefaultFormatIndices(TFormatIndices *formatIndices);
+
+/* lib/map.h:49-99 (defs lib/mapOps.h:35-168) */
+void free_map(Map *map);
+void new_pixmap(Map *map, unsigned int width, unsigned int height, unsigned int depth);
+void new_bytemap(Map *map, unsigned int width, unsigned int height);
+void new_intmap(Map *map, unsigned int width, unsigned int height);
+void new_coordmap(Map *map, unsigned int width, unsigned int height);
+void set_bytemap(Map *map, unsigned char value);
+void invert_bytemap(Map *map);
+void interleave_mask(Map *pixmap, Map *mask);
+
+/* ------------------------------------------------------------- extensions */
+/* Not in the reference: mode selection, statistics, state access and the
+ * device-resident path used for throughput measurement. */
+
+typedef enum {
+  /* Dependency wavefronts: each pass runs as batches of target pixels that are
+   * synthesized in parallel; candidates are neighbour-source propagation plus
+   * counter-based random probes.  The default. */
+  RESYNTH_MODE_WAVEFRONT = 0,
+  /* Sequential replay: target pixels are visited one at a time in the
+   * reference's order with the reference's PRNG stream; the output is
+   * byte-identical to the reference's single-threaded engine. */
+  RESYNTH_MODE_REPLAY = 1
+} TResynthMode;
+
+typedef struct {
+  int mode;                   /* TResynthMode */
+  unsigned int seed;          /* wavefront probe RNG seed (0 = 1198472) */
+  unsigned int firstBatch;    /* wavefront: pass-0 first batch size (0 = default) */
+  unsigned int refineBatches; /* wavefront: sequential batches per refinement pass (0 = default) */
+  unsigned int warpsPerBlock; /* wavefront: 0 = autotuned */
+  int recordState;            /* keep final sourceOf/hasValue for resynthGetState() */
+  int profile;                /* time each synthesis-kernel launch with CUDA events (stats.waveMs) */
+  unsigned int phaseSide;     /* wavefront: k of the k x k colour phases (0 = from the patch radius, 1 = none) */
+  unsigned int bandGrowth;    /* wavefront: pass-0 band growth in percent for random orders (0 = 200) */
+} TResynthOptions;
+
+typedef struct {
+  unsigned long long visits;      /* target-pixel visits over all passes */
+  unsigned long long evals;       /* candidate patches scored */
+  unsigned long long terms;       /* neighbour terms evaluated (after early-out) */
+  unsigned int passes;
+  unsigned int passLength[6];
+  unsigned int betters[6];
+  unsigned int launches;          /* kernels launched by this call */
+  double deviceMs;                /* GPU time of the synthesis kernels (CUDA events) */
+  double totalMs;                 /* wall time of the call */
+  unsigned long long h2dBytes, d2hBytes;
+  double waveMs;                  /* profile: summed duration of the per-target synthesis kernels */
+  unsigned int waveLaunches;      /* profile: how many launches waveMs covers */
+  unsigned long long waveTerms;   /* profile: neighbour terms those launches evaluated */
+} TResynthStats;
+
+/* Default options (wavefront mode, or the mode named by the environment
+ * variable RESYNTH_MODE=replay|wavefront). */
+void resynthDefaultOptions(TResynthOptions *options);
+
+/* Sets the mode imageSynth/imageSynth2/engine use in this process.
+ * Returns the previous mode, or -1 for an unknown mode. */
+int resynthSetMode(int mode);
+
+/* engine() with options and statistics.  stats may be NULL. */
+int engineEx(const TImageSynthParameters *parameters, const TFormatIndices *indices, Map *targetMap,
+             Map *corpusMap, void (*progressCallback)(int, void *), void *contextInfo, int *cancelFlag,
+             const TResynthOptions *options, TResynthStats *stats);
+
+/* imageSynth() with options and statistics (mask2 may be NULL). */
+int imageSynthEx(ImageBuffer *imageBuffer, ImageBuffer *mask, ImageBuffer *mask2, TImageFormat imageFormat,
+                 TImageSynthParameters *parameters, void (*progressCallback)(int, void *), void *contextInfo,
+                 int *cancelFlag, const TResynthOptions *options, TResynthStats *stats);
+
+/* Final state of the last engineEx/imageSynthEx call on this thread that ran
+ * with options->recordState: sourceOf (width*height Coordinates, (-1,-1) = none)
+ * and hasValue (width*height bytes) of the target.  Returns 0 or an error. */
+int resynthGetState(Coordinates *sourceOf, unsigned char *hasValue, unsigned int width, unsigned int height);
+
+/* Same as engineEx on pixmaps that already live in device memory (the
+ * interleaved layout of Map data).  dTarget is updated in place.  stream is a
+ * cudaStream_t (NULL = the library's stream).  Progress callbacks and cancel
+ * behave as in engineEx. */
+int engineDevice(const TImageSynthParameters *parameters, const TFormatIndices *indices,
+                 unsigned char *dTarget, unsigned int targetWidth, unsigned int targetHeight,
+                 const unsigned char *dCorpus, unsigned int corpusWidth, unsigned int corpusHeight,
+                 void *stream, void (*progressCallback)(int, void *), void *contextInfo, int *cancelFlag,
+                 const TResynthOptions *options, TResynthStats *stats);
+
+/* Frozen-state best fit.  For each target point, the patch is built from the
+ * given frozen state exactly as the reference's prepare_neighbors
+ * (lib/synthesize.h:189-241), and the candidates candidates[candStart[t] ..
+ * candStart[t+1]) are scored in order with the reference's computeBestFit rule
+ * (lib/synthesize.h:266-400: strict-less update from UINT_MAX).  Outputs per
+ * target: bestSum (UINT_MAX if no candidate), bestPoint ((-1,-1) if none) and
+ * patchCount (neighbours in the patch).  All pointers are host memory;
+ * target/corpus are interleaved pixmaps, hasValue/sourceOf are target-sized. */
+int resynthFrozenBestFit(const TImageSynthParameters *parameters, const TFormatIndices *indices,
+                         const unsigned char *target, unsigned int targetWidth, unsigned int targetHeight,
+                         const unsigned char *corpus, unsigned int corpusWidth, unsigned int corpusHeight,
+                         const unsigned char *hasValue, const Coordinates *sourceOf,
+                         const Coordinates *targets, unsigned int targetCount,
+                         const unsigned int *candStart, const Coordinates *candidates,
+                         unsigned int *bestSum, Coordinates *bestPoint, unsigned int *patchCount);
+
+/* Patch energy of a final state: the sum over targets of the full-patch metric
+ * (no early-out) at each target's source, patches built from the given state.
+ * perTarget (may be NULL) receives each target's term. */
+int resynthPatchEnergy(const TImageSynthParameters *parameters, const TFormatIndices *indices,
+                       const unsigned char *target, unsigned int targetWidth, unsigned int targetHeight,
+                       const unsigned char *corpus, unsigned int corpusWidth, unsigned int corpusHeight,
+                       const unsigned char *hasValue, const Coordinates *sourceOf,
+                       const Coordinates *targets, unsigned int targetCount,
+                       unsigned long long *energy, unsigned int *perTarget);
+
+/* Text of the last error on this thread ("" if none). */
+const char *resynthLastError(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

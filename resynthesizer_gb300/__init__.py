@@ -1,0 +1,301 @@
+"""resynthesizer_gb300 -- GB300 texture-synthesis engine (Python side of libresynthesizer.so).
+
+The engine itself is the C ABI library built from resynthesizer_gb300/csrc
+(see include/resynthesizer.h); this module loads it with ctypes and mirrors
+the reference's API for Python callers and tests:
+
+    image_synth(image, mask, fmt, params)       -- imageSynth / imageSynth2
+    engine(target, corpus, fmt_spec, params)    -- engine() on interleaved pixmaps
+    frozen_best_fit(...), patch_energy(...)     -- state-level extensions
+
+There is no CPU fallback: if the library is missing, importing succeeds but
+every call raises; if no GPU is usable, calls return RESYNTH_ERROR_DEVICE.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libresynthesizer.so")
+
+T_RGB, T_RGBA, T_Gray, T_GrayA = 0, 1, 2, 3
+MODE_WAVEFRONT, MODE_REPLAY = 0, 1
+ERRORS = {0: "SUCCESS", 1: "INVALID_IMAGE_FORMAT", 2: "IMAGE_MASK_MISMATCH", 3: "PATCH_SIZE_EXCEEDED",
+          4: "MATCH_CONTEXT_TYPE_RANGE", 5: "EMPTY_TARGET", 6: "EMPTY_CORPUS", 100: "DEVICE", 101: "UNSUPPORTED",
+          102: "ARGUMENT"}
+
+
+class ImageSynthParameters(C.Structure):
+    """TImageSynthParameters (lib/engineParams.h:31-86)."""
+    _fields_ = [("isMakeSeamlesslyTileableHorizontally", C.c_int), ("isMakeSeamlesslyTileableVertically", C.c_int),
+                ("matchContextType", C.c_int), ("mapWeight", C.c_double), ("sensitivityToOutliers", C.c_double),
+                ("patchSize", C.c_uint), ("maxProbeCount", C.c_uint)]
+
+
+class FormatIndices(C.Structure):
+    """TFormatIndices (lib/imageFormatIndicies.h:46-58)."""
+    _fields_ = [("colorEndBip", C.c_ubyte), ("alpha_bip", C.c_ubyte), ("map_start_bip", C.c_ubyte),
+                ("map_end_bip", C.c_ubyte), ("img_match_bpp", C.c_ubyte), ("map_match_bpp", C.c_ubyte),
+                ("total_bpp", C.c_ubyte), ("isAlphaTarget", C.c_int), ("isAlphaSource", C.c_int)]
+
+
+class ImageBuffer(C.Structure):
+    _fields_ = [("data", C.POINTER(C.c_ubyte)), ("width", C.c_uint), ("height", C.c_uint), ("rowBytes", C.c_size_t)]
+
+
+class GArray(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("len", C.c_uint)]
+
+
+class Map(C.Structure):
+    _fields_ = [("width", C.c_uint), ("height", C.c_uint), ("depth", C.c_uint), ("data", C.POINTER(GArray))]
+
+
+class Options(C.Structure):
+    _fields_ = [("mode", C.c_int), ("seed", C.c_uint), ("firstBatch", C.c_uint), ("refineBatches", C.c_uint),
+                ("warpsPerBlock", C.c_uint), ("recordState", C.c_int), ("profile", C.c_int),
+                ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("visits", C.c_ulonglong), ("evals", C.c_ulonglong), ("terms", C.c_ulonglong),
+                ("passes", C.c_uint), ("passLength", C.c_uint * 6), ("betters", C.c_uint * 6),
+                ("launches", C.c_uint), ("deviceMs", C.c_double), ("totalMs", C.c_double),
+                ("h2dBytes", C.c_ulonglong), ("d2hBytes", C.c_ulonglong), ("waveMs", C.c_double),
+                ("waveLaunches", C.c_uint), ("waveTerms", C.c_ulonglong)]
+
+    def as_dict(self) -> dict:
+        return dict(visits=self.visits, evals=self.evals, terms=self.terms, passes=self.passes,
+                    passLength=list(self.passLength)[: self.passes], betters=list(self.betters)[: self.passes],
+                    launches=self.launches, deviceMs=self.deviceMs, totalMs=self.totalMs,
+                    h2dBytes=self.h2dBytes, d2hBytes=self.d2hBytes, waveMs=self.waveMs,
+                    waveLaunches=self.waveLaunches, waveTerms=self.waveTerms)
+
+
+PROGRESS = C.CFUNCTYPE(None, C.c_int, C.c_void_p)
+
+_lib = None
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def lib() -> C.CDLL:
+    """The loaded libresynthesizer.so; raises if it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing(f"{LIB_PATH} not built: run `python -m resynthesizer_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        vp, u, P = C.c_void_p, C.c_uint, C.POINTER
+        L.imageSynth.argtypes = [P(ImageBuffer), P(ImageBuffer), C.c_int, P(ImageSynthParameters), vp, vp, P(C.c_int)]
+        L.imageSynth2.argtypes = [P(ImageBuffer), P(ImageBuffer), P(ImageBuffer), C.c_int, P(ImageSynthParameters),
+                                  vp, vp, P(C.c_int)]
+        L.imageSynthEx.argtypes = [P(ImageBuffer), P(ImageBuffer), P(ImageBuffer), C.c_int, P(ImageSynthParameters),
+                                   vp, vp, P(C.c_int), P(Options), P(Stats)]
+        L.engine.argtypes = [ImageSynthParameters, P(FormatIndices), P(Map), P(Map), vp, vp, P(C.c_int)]
+        L.engineEx.argtypes = [P(ImageSynthParameters), P(FormatIndices), P(Map), P(Map), vp, vp, P(C.c_int),
+                               P(Options), P(Stats)]
+        L.engineDevice.argtypes = [P(ImageSynthParameters), P(FormatIndices), vp, u, u, vp, u, u, vp, vp, vp,
+                                   P(C.c_int), P(Options), P(Stats)]
+        L.resynthFrozenBestFit.argtypes = [P(ImageSynthParameters), P(FormatIndices), vp, u, u, vp, u, u, vp, vp, vp,
+                                           u, vp, vp, vp, vp, vp]
+        L.resynthPatchEnergy.argtypes = [P(ImageSynthParameters), P(FormatIndices), vp, u, u, vp, u, u, vp, vp, vp, u,
+                                         P(C.c_ulonglong), vp]
+        L.resynthGetState.argtypes = [vp, vp, u, u]
+        L.resynthLastError.restype = C.c_char_p
+        L.resynthSetMode.argtypes = [C.c_int]
+        L.resynthDefaultOptions.argtypes = [P(Options)]
+        L.prepareImageFormatIndices.argtypes = [P(FormatIndices), u, u, C.c_int, C.c_int, C.c_int]
+        L.prepareImageFormatIndicesFromFormatType.argtypes = [P(FormatIndices), C.c_int]
+        L.countPixelelsPerPixelForFormat.argtypes = [C.c_int]
+        L.countPixelelsPerPixelForFormat.restype = C.c_uint
+        L.setDefaultParams.argtypes = [P(ImageSynthParameters)]
+        for name in ("new_pixmap",):
+            getattr(L, name).argtypes = [P(Map), u, u, u]
+        for name in ("new_bytemap", "new_intmap", "new_coordmap"):
+            getattr(L, name).argtypes = [P(Map), u, u]
+        L.free_map.argtypes = [P(Map)]
+        L.set_bytemap.argtypes = [P(Map), C.c_ubyte]
+        L.invert_bytemap.argtypes = [P(Map)]
+        L.interleave_mask.argtypes = [P(Map), P(Map)]
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().resynthLastError().decode()
+
+
+def params(tileH=0, tileV=0, matchContextType=1, mapWeight=0.5, sensitivity=0.117, patchSize=30,
+           maxProbeCount=200) -> ImageSynthParameters:
+    return ImageSynthParameters(tileH, tileV, matchContextType, mapWeight, sensitivity, patchSize, maxProbeCount)
+
+
+def default_params() -> ImageSynthParameters:
+    p = ImageSynthParameters()
+    lib().setDefaultParams(C.byref(p))
+    return p
+
+
+def format_indices(colors, mapColors=0, alphaTarget=0, alphaSource=0, isMap=0) -> FormatIndices:
+    f = FormatIndices()
+    lib().prepareImageFormatIndices(C.byref(f), colors, mapColors, alphaTarget, alphaSource, isMap)
+    return f
+
+
+def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, recordState=0,
+            profile=0, phaseSide=0, bandGrowth=0) -> Options:
+    o = Options()
+    lib().resynthDefaultOptions(C.byref(o))
+    if mode is not None:
+        o.mode = mode
+    o.seed, o.firstBatch, o.refineBatches, o.warpsPerBlock, o.recordState, o.profile = (
+        seed, firstBatch, refineBatches, warpsPerBlock, recordState, profile)
+    o.phaseSide, o.bandGrowth = phaseSide, bandGrowth
+    return o
+
+
+def _vp(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _buf(a: np.ndarray) -> ImageBuffer:
+    h, w = a.shape[:2]
+    bpp = a.shape[2] if a.ndim == 3 else 1
+    return ImageBuffer(a.ctypes.data_as(C.POINTER(C.c_ubyte)), w, h, w * bpp)
+
+
+@dataclass
+class Result:
+    rc: int
+    out: np.ndarray
+    stats: dict
+    source: np.ndarray | None = None
+    has_value: np.ndarray | None = None
+
+
+def image_synth(image, mask, fmt, p: ImageSynthParameters | None = None, mask2=None, opts: Options | None = None,
+                cancel=0, progress=None, raw_entry=False) -> Result:
+    """Simple API on an (H, W, bpp) image and (H, W) mask.  raw_entry=True
+    calls the reference-named imageSynth/imageSynth2 entry point itself."""
+    img = np.ascontiguousarray(image, np.uint8).copy()
+    m = np.ascontiguousarray(mask, np.uint8)
+    ib, mb = _buf(img), _buf(m)
+    m2 = None
+    if mask2 is not None:
+        m2a = np.ascontiguousarray(mask2, np.uint8)
+        m2 = _buf(m2a)
+    cf = C.c_int(cancel)
+    cb = PROGRESS(progress) if progress else None
+    cbp = C.cast(cb, C.c_void_p) if cb else None
+    pp = C.byref(p) if p is not None else None
+    st = Stats()
+    if raw_entry:
+        if m2 is None:
+            rc = lib().imageSynth(C.byref(ib), C.byref(mb), fmt, pp, cbp, None, C.byref(cf))
+        else:
+            rc = lib().imageSynth2(C.byref(ib), C.byref(mb), C.byref(m2), fmt, pp, cbp, None, C.byref(cf))
+    else:
+        rc = lib().imageSynthEx(C.byref(ib), C.byref(mb), C.byref(m2) if m2 else None, fmt, pp, cbp, None,
+                                C.byref(cf), C.byref(opts) if opts else None, C.byref(st))
+    r = Result(rc, img, st.as_dict())
+    if opts is not None and opts.recordState and rc == 0:
+        h, w = m.shape
+        r.source, r.has_value = get_state(w, h)
+    return r
+
+
+class PixmapMap:
+    """A reference Map (lib/map.h:28-33) owning a copy of an (H, W, depth) pixmap."""
+
+    def __init__(self, pix: np.ndarray):
+        h, w, d = pix.shape
+        self.map = Map()
+        lib().new_pixmap(C.byref(self.map), w, h, d)
+        C.memmove(self.map.data.contents.data, np.ascontiguousarray(pix, np.uint8).ctypes.data, pix.nbytes)
+        self.shape = pix.shape
+
+    def array(self) -> np.ndarray:
+        n = int(np.prod(self.shape))
+        buf = (C.c_ubyte * n).from_address(self.map.data.contents.data)
+        return np.frombuffer(buf, np.uint8, n).reshape(self.shape).copy()
+
+    def __del__(self):
+        try:
+            lib().free_map(C.byref(self.map))
+        except Exception:
+            pass
+
+
+def engine(target, corpus, fmt: FormatIndices, p: ImageSynthParameters, opts: Options | None = None, cancel=0,
+           progress=None, raw_entry=False) -> Result:
+    """engine() on interleaved pixmaps (H, W, total_bpp); returns the updated target."""
+    tm, cm = PixmapMap(target), PixmapMap(corpus)
+    cf = C.c_int(cancel)
+    cb = PROGRESS(progress) if progress else None
+    cbp = C.cast(cb, C.c_void_p) if cb else None
+    st = Stats()
+    if raw_entry:
+        rc = lib().engine(p, C.byref(fmt), C.byref(tm.map), C.byref(cm.map), cbp, None, C.byref(cf))
+    else:
+        rc = lib().engineEx(C.byref(p), C.byref(fmt), C.byref(tm.map), C.byref(cm.map), cbp, None, C.byref(cf),
+                            C.byref(opts) if opts else None, C.byref(st))
+    r = Result(rc, tm.array(), st.as_dict())
+    if opts is not None and opts.recordState and rc == 0:
+        h, w = target.shape[:2]
+        r.source, r.has_value = get_state(w, h)
+    return r
+
+
+def get_state(w, h):
+    src = np.zeros((h, w, 2), np.int32)
+    hv = np.zeros((h, w), np.uint8)
+    rc = lib().resynthGetState(_vp(src), _vp(hv), w, h)
+    if rc:
+        raise RuntimeError(f"resynthGetState: {last_error()}")
+    return src, hv
+
+
+def engine_device(p, fmt, d_target: int, tw, th, d_corpus: int, cw, ch, stream: int = 0,
+                  opts: Options | None = None) -> tuple[int, dict]:
+    """engineDevice on device pointers (e.g. torch tensors' data_ptr())."""
+    st = Stats()
+    rc = lib().engineDevice(C.byref(p), C.byref(fmt), C.c_void_p(d_target), tw, th, C.c_void_p(d_corpus), cw, ch,
+                            C.c_void_p(stream) if stream else None, None, None, None,
+                            C.byref(opts) if opts else None, C.byref(st))
+    return rc, st.as_dict()
+
+
+def frozen_best_fit(p, fmt, target, corpus, has_value, source, targets, cand_start, cands):
+    th, tw, _ = target.shape
+    ch, cw, _ = corpus.shape
+    n = len(targets)
+    out_sum = np.zeros(n, np.uint32)
+    out_pt = np.zeros((n, 2), np.int32)
+    out_cnt = np.zeros(n, np.uint32)
+    a = [np.ascontiguousarray(x) for x in (target, corpus, has_value, source, targets, cand_start, cands)]
+    rc = lib().resynthFrozenBestFit(C.byref(p), C.byref(fmt), _vp(a[0]), tw, th, _vp(a[1]), cw, ch, _vp(a[2]),
+                                    _vp(a[3]), _vp(a[4]), n, _vp(a[5]), _vp(a[6]), _vp(out_sum), _vp(out_pt),
+                                    _vp(out_cnt))
+    if rc:
+        raise RuntimeError(f"resynthFrozenBestFit rc={rc}: {last_error()}")
+    return out_sum, out_pt, out_cnt
+
+
+def patch_energy(p, fmt, target, corpus, has_value, source, targets):
+    th, tw, _ = target.shape
+    ch, cw, _ = corpus.shape
+    per = np.zeros(len(targets), np.uint32)
+    e = C.c_ulonglong(0)
+    a = [np.ascontiguousarray(x) for x in (target, corpus, has_value, source, targets)]
+    rc = lib().resynthPatchEnergy(C.byref(p), C.byref(fmt), _vp(a[0]), tw, th, _vp(a[1]), cw, ch, _vp(a[2]),
+                                  _vp(a[3]), _vp(a[4]), len(targets), C.byref(e), _vp(per))
+    if rc:
+        raise RuntimeError(f"resynthPatchEnergy rc={rc}: {last_error()}")
+    return int(e.value), per

@@ -1,0 +1,1164 @@
+// synth_host.cpp -- the C ABI of libresynthesizer.so: the reference-compatible
+// entry points (imageSynth, imageSynth2, engine, map and format helpers) and
+// the extensions declared in include/resynthesizer.h.
+//
+// Host work mirrors the reference's preparation (lib/engine.c:338-497,
+// 539-690): target/corpus point lists, hasValue, sourceOf, sorted offsets,
+// metric tables and the target order with the reference's PRNG stream.  The
+// passes run on the GPU (synth_kernels.cu) in one of two modes:
+//   replay     -- one CTA visits targets in the reference order, consuming the
+//                 same PRNG stream: output identical to the reference's
+//                 single-threaded engine;
+//   wavefront  -- each pass runs as batches of targets synthesized in parallel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/resynthesizer.h"
+#include "synth_internal.h"
+
+#define RS_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+// ------------------------------------------------------------------ errors
+
+thread_local std::string g_lastError;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_lastError = buf;
+  if (code == RESYNTH_ERROR_DEVICE) fprintf(stderr, "resynthesizer: %s\n", buf);
+  return code;
+}
+
+struct CudaError {
+  cudaError_t e;
+  const char* what;
+};
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) throw CudaError{e_, #call};        \
+  } while (0)
+
+// -------------------------------------------------------- reference PRNG
+
+// The PRNG of the reference's standalone build is libc srand/rand
+// (lib/glibProxy.c:29-49).  This is glibc's TYPE_3 additive feedback
+// generator, restated so the stream can be produced without touching the
+// process-wide rand() state: r[0] = seed, r[i] = 16807 r[i-1] mod (2^31 - 1)
+// for i < 31, r[i] = r[i-31] for i in 31..33, then r[i] = r[i-3] + r[i-31]
+// (mod 2^32); the k-th output is r[k + 344] >> 1.
+class GlibcRand {
+ public:
+  explicit GlibcRand(unsigned seed) {
+    int32_t r[34];
+    r[0] = seed ? (int32_t)seed : 1;
+    for (int i = 1; i < 31; i++) {
+      const int64_t v = (16807LL * r[i - 1]) % 2147483647LL;
+      r[i] = (int32_t)(v < 0 ? v + 2147483647LL : v);
+    }
+    for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+    for (int i = 0; i < 34; i++) ring_[i] = (uint32_t)r[i];
+    pos_ = 34;
+    for (int i = 34; i < 344; i++) step();
+  }
+  int next() { return (int)(step() >> 1); }
+  // lib/glibProxy.c:36-49 (no draw when the bound is below 1)
+  unsigned range(unsigned lo, unsigned hiExcl) {
+    if (hiExcl < 1) return 0;
+    const unsigned hi = hiExcl - 1;
+    return lo + (unsigned)next() / (2147483647u / (hi - lo + 1) + 1);
+  }
+
+ private:
+  uint32_t step() {
+    const uint32_t v = ring_[(pos_ - 31) % 34] + ring_[(pos_ - 3) % 34];
+    ring_[pos_ % 34] = v;
+    pos_++;
+    return v;
+  }
+  uint32_t ring_[34];
+  uint64_t pos_;
+};
+
+// --------------------------------------------------------------- formats
+
+void format_indices(TFormatIndices* f, unsigned colors, unsigned mapColors, int alphaT, int alphaS,
+                    int isMap) {
+  // lib/imageFormat.c:116-207
+  f->img_match_bpp = (TPixelelIndex)colors;
+  f->colorEndBip = (TPixelelIndex)(1 + colors);
+  if (alphaT || alphaS) {
+    f->alpha_bip = f->colorEndBip;
+    f->map_start_bip = (TPixelelIndex)(f->colorEndBip + 1);
+  } else {
+    f->map_start_bip = f->colorEndBip;
+  }
+  f->map_match_bpp = (TPixelelIndex)(isMap ? mapColors : 0);
+  f->map_end_bip = (TPixelelIndex)(f->map_start_bip + f->map_match_bpp);
+  f->total_bpp = f->map_end_bip;
+  f->isAlphaTarget = alphaT;
+  f->isAlphaSource = alphaS;
+}
+
+// ------------------------------------------------------------- host prep
+
+struct Pt {
+  int x, y;
+};
+
+// Comparators of the reference (lib/engineTypes.h:51-149): they never return
+// 0, so the tie order is libc qsort's -- the reason ordering calls qsort.
+int cmp_less_cartesian(const void* va, const void* vb) {
+  const Pt *a = (const Pt*)va, *b = (const Pt*)vb;
+  return (a->y * a->y + a->x * a->x < b->y * b->y + b->x * b->x) ? -1 : 1;
+}
+int cmp_more_horizontal(const void* va, const void* vb) {
+  const Pt *a = (const Pt*)va, *b = (const Pt*)vb;
+  return (a->x * a->x < b->x * b->x) ? 1 : -1;
+}
+int cmp_less_horizontal(const void* va, const void* vb) {
+  const Pt *a = (const Pt*)va, *b = (const Pt*)vb;
+  return (a->x * a->x < b->x * b->x) ? -1 : 1;
+}
+int cmp_more_vertical(const void* va, const void* vb) {
+  const Pt *a = (const Pt*)va, *b = (const Pt*)vb;
+  return (a->y * a->y < b->y * b->y) ? 1 : -1;
+}
+int cmp_less_vertical(const void* va, const void* vb) {
+  const Pt *a = (const Pt*)va, *b = (const Pt*)vb;
+  return (a->y * a->y < b->y * b->y) ? -1 : 1;
+}
+struct SortElem {
+  Pt p;
+  float prop;
+};
+int cmp_less_inward(const void* va, const void* vb) {
+  return (((const SortElem*)va)->prop < ((const SortElem*)vb)->prop) ? -1 : 1;
+}
+int cmp_more_inward(const void* va, const void* vb) { return cmp_less_inward(va, vb) == 1 ? -1 : 1; }
+
+// Sorted offsets (lib/engine.c:465-497): all offsets of the (2w-1) x (2h-1)
+// box, w/h the smaller of target and corpus, ascending in x^2 + y^2.  The
+// reference sorts with libc qsort and a comparator that never returns 0; with
+// glibc's merge sort that leaves equal distances in reverse generation order,
+// i.e. descending y, then descending x.  Generated directly in that order
+// (checked against libc qsort by the tests), optionally truncated to radius^2.
+std::vector<int2> sorted_offsets(int w, int h, long long maxD2) {
+  std::vector<uint64_t> keys;
+  const int W = 2 * w - 1;
+  keys.reserve((size_t)W * (2 * h - 1));
+  for (int y = -h + 1; y < h; y++)
+    for (int x = -w + 1; x < w; x++) {
+      const long long d2 = (long long)x * x + (long long)y * y;
+      if (d2 > maxD2) continue;
+      const uint32_t idx = (uint32_t)((y + h - 1) * W + (x + w - 1));
+      keys.push_back(((uint64_t)d2 << 32) | (uint32_t)~idx);
+    }
+  std::sort(keys.begin(), keys.end());
+  std::vector<int2> out(keys.size());
+  for (size_t i = 0; i < keys.size(); i++) {
+    const uint32_t idx = ~(uint32_t)(keys[i] & 0xffffffffu);
+    out[i] = make_int2((int)(idx % W) - (w - 1), (int)(idx / W) - (h - 1));
+  }
+  return out;
+}
+
+// Metric tables (lib/matchWeighting.h:49-60, 142-178): float parameters,
+// double arithmetic, truncating casts -- computed on the host with libm.
+void metric_tables(double sensitivity, double mapWeight, uint32_t* ct, uint32_t* mt) {
+  const float c = (float)sensitivity, w = (float)mapWeight;
+  auto nlc = [c](double x) { return std::log((x / (c * 256)) * (x / (c * 256)) + 1.0); };
+  for (int i = -256; i < 256; i++) {
+    const double v = nlc(i) / nlc(256) * (float)65535;
+    ct[256 + i] = (unsigned short)v;
+    mt[256 + i] = (unsigned int)(i * i * w * 4.0);
+  }
+}
+
+Pt bbox_center(const std::vector<Pt>& v) {  // lib/engineTypes.h:187-226
+  int ulx = INT_MAX, uly = INT_MAX, lrx = 0, lry = 0;
+  for (const Pt& p : v) {
+    ulx = std::min(ulx, p.x);
+    uly = std::min(uly, p.y);
+    lrx = std::max(lrx, p.x);
+    lry = std::max(lry, p.y);
+  }
+  return Pt{(lrx - ulx) / 2 + ulx, (lry - uly) / 2 + uly};
+}
+
+unsigned ray_of(Pt a) {  // lib/brushfire.h:62-67
+  return (unsigned)(std::atan2((double)(float)a.y, (double)(float)a.x) * 200 /
+                        3.1415926535897932384626433832795028841971693993751 +
+                    200);
+}
+
+// The target order of lib/orderTarget.h:268-343, consuming `rng` exactly as
+// the reference does.  Returns 0 or MATCH_CONTEXT_TYPE_RANGE.
+int order_targets(int type, std::vector<Pt>& v, GlibcRand& rng) {
+  const unsigned n = (unsigned)v.size();
+  if (type == 0 || type == 1) {
+    for (unsigned i = 0; i < n; i++) std::swap(v[i], v[rng.range(0, n)]);
+    return 0;
+  }
+  if (type < 0 || type > 8) return IMAGE_SYNTH_ERROR_MATCH_CONTEXT_TYPE_RANGE;
+  const Pt c = bbox_center(v);
+  for (Pt& p : v) p = Pt{p.x - c.x, p.y - c.y};
+  if (type == 2 || type == 5 || type == 8) {
+    // Brushfire key: |p|^2 over the largest |q|^2 on the same one of 401 rays
+    // (lib/brushfire.h:73-148).  The squeeze order (type 8) writes its sorted
+    // array straight back, so it equals the inward order (lib/orderTarget.h:209-262).
+    unsigned maxr[401] = {0};
+    for (const Pt& p : v) {
+      const unsigned d = (unsigned)(p.x * p.x + p.y * p.y), r = ray_of(p);
+      if (d > maxr[r]) maxr[r] = d;
+    }
+    std::vector<SortElem> s(n);
+    for (unsigned i = 0; i < n; i++)
+      s[i] = SortElem{v[i], (float)(v[i].y * v[i].y + v[i].x * v[i].x) / maxr[ray_of(v[i])]};
+    std::qsort(s.data(), n, sizeof(SortElem), type == 5 ? cmp_less_inward : cmp_more_inward);
+    for (unsigned i = 0; i < n; i++) v[i] = s[i].p;
+  } else {
+    auto cmp = type == 3 ? cmp_more_horizontal : type == 4 ? cmp_more_vertical
+             : type == 6 ? cmp_less_horizontal : cmp_less_vertical;
+    std::qsort(v.data(), n, sizeof(Pt), cmp);
+  }
+  for (Pt& p : v) p = Pt{p.x + c.x, p.y + c.y};
+  // banded shuffle, lib/orderTarget.h:58-79
+  const int last = (int)n - 1, half = (int)(n * 0.1);
+  for (int i = 0; i <= last; i++) {
+    const int lo = std::max(i - half, 0), hi = std::min(i + half, last);
+    std::swap(v[i], v[lo + (int)rng.range(0, (unsigned)(hi - lo))]);
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------ the problem
+
+struct HostPrep {
+  std::vector<Pt> targets;         // in visit order
+  std::vector<Pt> corpusPts;       // row-major
+  std::vector<uint8_t> hasValue;   // initial, target-sized
+  uint32_t ct[512], mt[512];
+  unsigned ends[rs::kPasses];
+  unsigned estimated;
+  GlibcRand rng{1198472u};         // engine.c:643, consumed by ordering first
+};
+
+// Pass lengths (lib/passes.h:67-93): all n targets twice, then prefixes of
+// 3/4 of the previous length; `estimated` is their sum (lib/passes.h:55-63).
+void pass_schedule(unsigned n, unsigned ends[rs::kPasses], unsigned& estimated) {
+  ends[0] = n;
+  estimated = n;
+  for (int i = 1; i < rs::kPasses; i++) {
+    ends[i] = n;
+    estimated += n;
+    n = n * 3 / 4;
+  }
+}
+
+// Engine preparation (lib/engine.c:585-645).  Returns 0 or an engine error.
+int prepare(const TImageSynthParameters& p, const TFormatIndices& f, const uint8_t* target, unsigned tw,
+            unsigned th, const uint8_t* corpus, unsigned cw, unsigned ch, HostPrep& hp) {
+  if (p.patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+  const size_t tn = (size_t)tw * th, cn = (size_t)cw * ch;
+  hp.hasValue.assign(tn, 0);
+  hp.targets.clear();
+  const int bpp = f.total_bpp;
+  for (unsigned y = 0; y < th; y++)
+    for (unsigned x = 0; x < tw; x++) {
+      const uint8_t* px = target + ((size_t)y * tw + x) * bpp;
+      const bool selected = px[0] != 0;
+      const bool opaque = f.isAlphaTarget ? px[f.alpha_bip] != 0 : true;
+      hp.hasValue[(size_t)y * tw + x] = (p.matchContextType && !selected && opaque) ? 1 : 0;
+      if (selected) hp.targets.push_back(Pt{(int)x, (int)y});
+    }
+  if (hp.targets.empty()) return IMAGE_SYNTH_ERROR_EMPTY_TARGET;
+  hp.corpusPts.clear();
+  hp.corpusPts.reserve(cn / 2);
+  for (unsigned y = 0; y < ch; y++)
+    for (unsigned x = 0; x < cw; x++) {
+      const uint8_t* px = corpus + ((size_t)y * cw + x) * bpp;
+      if (px[0] == 0xFF && (f.isAlphaSource ? px[f.alpha_bip] != 0 : true)) hp.corpusPts.push_back(Pt{(int)x, (int)y});
+    }
+  if (hp.corpusPts.empty()) return IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
+  metric_tables(p.sensitivityToOutliers, p.mapWeight, hp.ct, hp.mt);
+  hp.rng = GlibcRand(1198472u);
+  const int rc = order_targets(p.matchContextType, hp.targets, hp.rng);
+  if (rc) return rc;
+  pass_schedule((unsigned)hp.targets.size(), hp.ends, hp.estimated);
+  return 0;
+}
+
+// Progress emulation: lib/progress.c:53-65 called at every target index that
+// is a multiple of 4096 (lib/synthesize.h:493), before that index is visited.
+struct Progress {
+  unsigned estimated = 1, completed = 0, prior = 0;
+  void (*cb)(int, void*) = nullptr;
+  void* ctx = nullptr;
+  void tick() {
+    completed += 4095u;
+    const unsigned pct = (unsigned)(((float)completed / estimated) * 100);
+    if (pct > prior) {
+      if (cb) cb((int)pct, ctx);
+      prior = pct;
+    }
+  }
+};
+
+// ----------------------------------------------------------- device state
+
+struct Stream {
+  cudaStream_t s = nullptr;
+  volatile int* abortHost = nullptr;
+  int* abortDev = nullptr;
+  rs::Counters* hostCtr = nullptr;   // pinned: counter read-backs stay asynchronous
+  int* hostInts = nullptr;           // pinned: small read-backs
+  Stream() {
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CK(cudaHostAlloc((void**)&abortHost, sizeof(int), cudaHostAllocMapped));
+    *abortHost = 0;
+    CK(cudaHostGetDevicePointer((void**)&abortDev, (void*)abortHost, 0));
+    CK(cudaHostAlloc((void**)&hostCtr, sizeof(rs::Counters), cudaHostAllocDefault));
+    CK(cudaHostAlloc((void**)&hostInts, 16 * sizeof(int), cudaHostAllocDefault));
+  }
+};
+
+Stream& thread_stream() {
+  thread_local std::unique_ptr<Stream> st;
+  if (!st) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) throw CudaError{cudaErrorNoDevice, "no CUDA device"};
+    static std::once_flag poolOnce;
+    std::call_once(poolOnce, [] {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      }
+    });
+    st.reset(new Stream());
+  }
+  return *st;
+}
+
+// Stream-ordered device allocations released at scope exit.
+class Arena {
+ public:
+  explicit Arena(cudaStream_t s) : s_(s) {}
+  ~Arena() {
+    for (void* p : ptrs_) cudaFreeAsync(p, s_);
+  }
+  template <class T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    CK(cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T) + 16, s_));
+    ptrs_.push_back(p);
+    return static_cast<T*>(p);
+  }
+  template <class T>
+  T* upload(const T* h, size_t n, unsigned long long& bytes) {
+    T* d = alloc<T>(n);
+    if (n) CK(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, s_));
+    bytes += n * sizeof(T);
+    return d;
+  }
+
+ private:
+  cudaStream_t s_;
+  std::vector<void*> ptrs_;
+};
+
+// Cached sorted-offset lists (they depend only on the box and the radius).
+const std::vector<int2>& cached_offsets(int w, int h, long long maxD2) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, long long>, std::vector<int2>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_tuple(w, h, maxD2);
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    if (cache.size() > 16) cache.clear();
+    it = cache.emplace(key, sorted_offsets(w, h, maxD2)).first;
+  }
+  return it->second;
+}
+
+struct RecordedState {
+  std::vector<int2> src;
+  std::vector<uint8_t> has;
+  unsigned w = 0, h = 0;
+};
+thread_local RecordedState g_state;
+
+int g_defaultMode = -1;
+
+int default_mode() {
+  if (g_defaultMode < 0) {
+    const char* e = getenv("RESYNTH_MODE");
+    g_defaultMode = (e && !strcmp(e, "replay")) ? RESYNTH_MODE_REPLAY : RESYNTH_MODE_WAVEFRONT;
+  }
+  return g_defaultMode;
+}
+
+bool supported_format(const TFormatIndices& f) {
+  return f.img_match_bpp >= 1 && f.img_match_bpp <= 3 && f.map_match_bpp <= 3 && f.total_bpp <= 8 &&
+         f.colorEndBip == 1 + f.img_match_bpp;
+}
+
+// Device problem built from device pixmaps.
+struct DeviceProblem {
+  rs::Problem pb{};
+  uint32_t* tpx = nullptr;
+  uint32_t* tmap = nullptr;
+};
+
+DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameters& p, const TFormatIndices& f,
+                           const uint8_t* dT, unsigned tw, unsigned th, const uint8_t* dC, unsigned cw, unsigned ch,
+                           const uint8_t* hasInit, const int2* srcInit,
+                           const std::vector<int2>& offs, long long maxD2, unsigned long long& h2d,
+                           unsigned& launches) {
+  DeviceProblem d;
+  rs::Problem& pb = d.pb;
+  pb.tw = (int)tw;
+  pb.th = (int)th;
+  pb.cw = (int)cw;
+  pb.ch = (int)ch;
+  pb.nc = f.img_match_bpp;
+  pb.nm = f.map_match_bpp;
+  const size_t tn = (size_t)tw * th, cn = (size_t)cw * ch, cnPad = (cn + 3) & ~(size_t)3;
+  d.tpx = ar.alloc<uint32_t>(tn);
+  d.tmap = pb.nm ? ar.alloc<uint32_t>(tn) : nullptr;
+  uint32_t* cpx = ar.alloc<uint32_t>(cnPad);
+  uint32_t* cmap = pb.nm ? ar.alloc<uint32_t>(cnPad) : nullptr;
+  CK(rs_launch_pack(dT, (int)tw, (int)th, f.total_bpp, 1, pb.nc, f.map_start_bip, pb.nm, d.tpx, d.tmap, s));
+  CK(rs_launch_pack(dC, (int)cw, (int)ch, f.total_bpp, 1, pb.nc, f.map_start_bip, pb.nm, cpx, cmap, s));
+  launches += 2;
+  pb.tpx = d.tpx;
+  pb.tmap = d.tmap;
+  pb.cpx = cpx;
+  pb.cmap = cmap;
+  if (hasInit) {
+    pb.has = ar.upload(hasInit, tn, h2d);
+  } else {
+    pb.has = ar.alloc<uint8_t>(tn);
+  }
+  int2* src = ar.alloc<int2>(tn);
+  if (srcInit) {
+    CK(cudaMemcpyAsync(src, srcInit, tn * sizeof(int2), cudaMemcpyHostToDevice, s));
+    h2d += tn * sizeof(int2);
+  } else {
+    CK(cudaMemsetAsync(src, 0xFF, tn * sizeof(int2), s));   // (-1, -1)
+  }
+  pb.src = src;
+  pb.boxW = (int)std::min(tw, cw);
+  pb.boxH = (int)std::min(th, ch);
+  pb.maxD2 = maxD2;
+  pb.offs = ar.upload(offs.data(), offs.size(), h2d);
+  pb.noffs = (int)offs.size();
+  pb.patchLimit = (int)std::max(p.patchSize, 2u);
+  pb.tileH = p.isMakeSeamlesslyTileableHorizontally ? 1 : 0;
+  pb.tileV = p.isMakeSeamlesslyTileableVertically ? 1 : 0;
+  uint32_t ct[512], mt[512];
+  metric_tables(p.sensitivityToOutliers, p.mapWeight, ct, mt);
+  pb.clipCost = 65535u * f.img_match_bpp + mt[0] * f.map_match_bpp;
+  pb.ctab = ar.upload(ct, 512, h2d);
+  pb.mtab = ar.upload(mt, 512, h2d);
+  return d;
+}
+
+// Radius (squared) of the offset list used by the wavefront mode: enough for
+// any dense patch; sparse early batches look this far for context.
+long long wave_radius2(int w, int h) {
+  const long long full = (long long)(w - 1) * (w - 1) + (long long)(h - 1) * (h - 1);
+  return std::min<long long>(full, 256LL * 256LL);
+}
+
+// CUDA-event timing of individual kernel launches on their own stream.
+class LaunchTimer {
+ public:
+  ~LaunchTimer() {
+    for (auto& p : ev_) {
+      cudaEventDestroy(p.first);
+      cudaEventDestroy(p.second);
+    }
+  }
+  void begin(cudaStream_t s) {
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    ev_.emplace_back(a, b);
+    CK(cudaEventRecord(a, s));
+  }
+  void end(cudaStream_t s) { CK(cudaEventRecord(ev_.back().second, s)); }
+  double total() const {
+    double t = 0;
+    for (auto& p : ev_) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, p.first, p.second) == cudaSuccess) t += ms;
+    }
+    return t;
+  }
+  unsigned count() const { return (unsigned)ev_.size(); }
+
+ private:
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_;
+};
+
+// Side k of the colour phases: one more than the radius of a dense patch
+// (the distance of its last offset), so two targets of one phase are never
+// inside each other's dense patch.
+int phase_side(const std::vector<int2>& offs, int patchLimit) {
+  const size_t i = std::min<size_t>(offs.size(), (size_t)patchLimit) - 1;
+  const double r = std::sqrt((double)offs[i].x * offs[i].x + (double)offs[i].y * offs[i].y);
+  return std::max(1, std::min(8, (int)std::floor(r) + 1));
+}
+
+void wait_stream(Stream& st, cudaEvent_t ev, int* cancel) {
+  while (true) {
+    const cudaError_t q = cudaEventQuery(ev);
+    if (q == cudaSuccess) return;
+    if (q != cudaErrorNotReady) throw CudaError{q, "cudaEventQuery"};
+    if (cancel && *cancel) *st.abortHost = 1;
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
+// The pass loop on device pixmaps.  dT is updated in place.  `prepared` is
+// the host preparation when the caller already made it (engine() on host maps).
+int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, uint8_t* dT, unsigned tw,
+                      unsigned th, const uint8_t* dC, unsigned cw, unsigned ch, HostPrep* prepared,
+                      cudaStream_t userStream, void (*progressCb)(int, void*), void* ctx,
+                      int* cancel, const TResynthOptions& opt, TResynthStats& stats) {
+  Stream& st = thread_stream();
+  cudaStream_t s = userStream ? userStream : st.s;
+  *st.abortHost = 0;
+  int zero = 0;
+  if (!cancel) cancel = &zero;
+  const bool replay = opt.mode == RESYNTH_MODE_REPLAY;
+  const bool randomOrder = p.matchContextType == 0 || p.matchContextType == 1;
+  // Wavefront runs with a random order prepare on the device; replay and the
+  // directional orders use the host preparation (the reference's exact order).
+  const bool devicePrep = !replay && randomOrder;
+  HostPrep local;
+  if (!devicePrep && !prepared) {
+    std::vector<uint8_t> tHost((size_t)tw * th * f.total_bpp), cHost((size_t)cw * ch * f.total_bpp);
+    CK(cudaMemcpyAsync(tHost.data(), dT, tHost.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cHost.data(), dC, cHost.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    stats.d2hBytes += tHost.size() + cHost.size();
+    const int rc = prepare(p, f, tHost.data(), tw, th, cHost.data(), cw, ch, local);
+    if (rc) return rc;
+    prepared = &local;
+  }
+  const int mw = (int)std::min(tw, cw), mh = (int)std::min(th, ch);
+  const long long maxD2 = replay ? LLONG_MAX : wave_radius2(mw, mh);
+  const std::vector<int2>& offs = cached_offsets(mw, mh, maxD2);
+
+  Arena ar(s);
+  unsigned long long h2d = 0;
+  unsigned launches = 0;
+  cudaEvent_t e0, e1, epass;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventCreateWithFlags(&epass, cudaEventDisableTiming));
+  CK(cudaEventRecord(e0, s));
+  DeviceProblem dp = make_problem(ar, s, p, f, dT, tw, th, dC, cw, ch, devicePrep ? nullptr : prepared->hasValue.data(),
+                                  nullptr, offs, maxD2, h2d, launches);
+  int2* dTargets = nullptr;
+  unsigned ntargets = 0, ends[rs::kPasses], estimated = 0;
+  bool noContext = true;
+  if (devicePrep) {
+    const size_t tn = (size_t)tw * th, cn = (size_t)cw * ch;
+    int* scratch = ar.alloc<int>((size_t)std::max(rs_prep_scratch_ints((int)tw, (int)th), rs_prep_scratch_ints((int)cw, (int)ch)));
+    int* dCounts = ar.alloc<int>(4);
+    dTargets = ar.alloc<int2>(tn);
+    int2* cpts = ar.alloc<int2>(cn);
+    CK(rs_prep_target(dT, (int)tw, (int)th, f.total_bpp, f.alpha_bip, f.isAlphaTarget ? 1 : 0,
+                      p.matchContextType ? 1 : 0, dp.pb.has, dp.pb.src, scratch, dTargets, dCounts, s));
+    CK(rs_prep_corpus(dC, (int)cw, (int)ch, f.total_bpp, f.alpha_bip, f.isAlphaSource ? 1 : 0, scratch, cpts,
+                      dCounts + 2, s));
+    launches += 6;
+    CK(cudaMemcpyAsync(st.hostInts, dCounts, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    ntargets = (unsigned)st.hostInts[0];
+    noContext = st.hostInts[1] == 0;
+    const int ncorpus = st.hostInts[2];
+    // lib/engine.c:605-627
+    if (!ntargets) return IMAGE_SYNTH_ERROR_EMPTY_TARGET;
+    if (!ncorpus) return IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
+    dp.pb.cpts = cpts;
+    dp.pb.ncorpus = ncorpus;
+    dp.pb.fullCorpus = (size_t)ncorpus == cn ? 1 : 0;
+    pass_schedule(ntargets, ends, estimated);
+  } else {
+    HostPrep& hp = *prepared;
+    ntargets = (unsigned)hp.targets.size();
+    dTargets = ar.upload(reinterpret_cast<const int2*>(hp.targets.data()), hp.targets.size(), h2d);
+    dp.pb.cpts = ar.upload(reinterpret_cast<const int2*>(hp.corpusPts.data()), hp.corpusPts.size(), h2d);
+    dp.pb.ncorpus = (int)hp.corpusPts.size();
+    dp.pb.fullCorpus = (size_t)dp.pb.ncorpus == (size_t)cw * ch ? 1 : 0;
+    noContext = std::find(hp.hasValue.begin(), hp.hasValue.end(), 1) == hp.hasValue.end();
+    std::copy(hp.ends, hp.ends + rs::kPasses, ends);
+    estimated = hp.estimated;
+  }
+  rs::Counters* ctr = ar.alloc<rs::Counters>(1);
+  CK(cudaMemsetAsync(ctr, 0, sizeof(rs::Counters), s));
+
+  Progress prog;
+  prog.estimated = estimated;
+  prog.cb = progressCb;
+  prog.ctx = ctx;
+  unsigned bettersTotal = 0;
+
+  if (replay) {
+    HostPrep& hp = *prepared;
+    // PRNG stream after the ordering draws; each visit draws at most trys.
+    unsigned long long visitsMax = 0;
+    for (int i = 0; i < rs::kPasses; i++) visitsMax += ends[i];
+    const unsigned long long need = visitsMax * p.maxProbeCount + 1;
+    if (need > (1ull << 30)) return fail(RESYNTH_ERROR_UNSUPPORTED, "replay mode: PRNG stream too long (%llu)", need);
+    std::vector<int> stream(need);
+    for (auto& v : stream) v = hp.rng.next();
+    rs::ReplayArgs ra{};
+    ra.pb = dp.pb;
+    ra.targets = dTargets;
+    ra.recentProber = ar.alloc<unsigned>((size_t)cw * ch);
+    CK(cudaMemsetAsync(ra.recentProber, 0xFF, (size_t)cw * ch * sizeof(unsigned), s));
+    ra.randStream = ar.upload(stream.data(), stream.size(), h2d);
+    ra.randCount = (unsigned)stream.size();
+    ra.trys = p.maxProbeCount;
+    ra.ctr = ctr;
+    rs::Counters& hc = *st.hostCtr;
+    memset(&hc, 0, sizeof hc);
+    for (int pass = 0; pass < rs::kPasses; pass++) {
+      const unsigned end = ends[pass];
+      const unsigned bettersBefore = hc.betters;
+      for (unsigned t0 = 0; t0 < end; t0 += 4096u) {
+        prog.tick();
+        if (*cancel) break;
+        const unsigned t1 = std::min(end, t0 + 4096u);
+        CK(rs_launch_replay(ra, (int)t0, (int)t1, s));
+        launches++;
+        CK(cudaEventRecord(epass, s));
+        wait_stream(st, epass, nullptr);
+      }
+      CK(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (hc.error) return fail(RESYNTH_ERROR_DEVICE, "replay kernel reported error %u", hc.error);
+      const unsigned betters = hc.betters - bettersBefore;
+      stats.passes = pass + 1;
+      stats.passLength[pass] = end;
+      stats.betters[pass] = betters;
+      bettersTotal += betters;
+      if ((float)betters / ntargets < 0.1) break;   // lib/refiner.h:111
+    }
+    stats.visits = 0;
+    for (unsigned i = 0; i < stats.passes; i++) stats.visits += stats.passLength[i];
+    stats.evals = hc.refEvals;
+    stats.terms = hc.terms;
+  } else {
+    rs::WaveArgs wa{};
+    wa.pb = dp.pb;
+    wa.trys = p.maxProbeCount;
+    wa.seed = opt.seed ? opt.seed : 1198472u;
+    wa.ctr = ctr;
+    wa.abortFlag = st.abortDev;
+    // Schedule defaults chosen by energy sweeps (random orders: a tiny first
+    // band of 16 pure-probe targets, bands growing 3x; directional orders:
+    // bands of at least 1024 in visit order).
+    const unsigned first = opt.firstBatch ? opt.firstBatch : (randomOrder ? 16u : 1024u);
+    const unsigned refine = opt.refineBatches ? opt.refineBatches : 1u;
+    const double growth = (opt.bandGrowth ? opt.bandGrowth : 300u) / 100.0;
+    const int k = opt.phaseSide ? (int)opt.phaseSide : phase_side(offs, dp.pb.patchLimit);
+    constexpr int kMaxBands = 64;
+    // While no pixel outside the current pass has a value, a batch's patches
+    // can come from the list of already-synthesized targets (cheap when short).
+    wa.sparseLimit2 = 4LL * dp.pb.patchLimit * (long long)ntargets;
+    const bool sparseOk = noContext && !dp.pb.tileH && !dp.pb.tileV;
+    wa.stageSrc = ar.alloc<int2>(ntargets);
+    int2* dPass = ar.alloc<int2>(ntargets);
+    int* dBandEnds = ar.alloc<int>(kMaxBands);
+    int* batchStart = ar.alloc<int>((size_t)kMaxBands * k * k + 1);
+    int* work = ar.alloc<int>(3 * (size_t)kMaxBands * k * k + 1 + ntargets);
+    wa.targets = dPass;
+    wa.batchStart = batchStart;
+    rs::Counters& hc = *st.hostCtr;
+    LaunchTimer prof;
+    for (int pass = 0; pass < rs::kPasses; pass++) {
+      const unsigned end = ends[pass];
+      // Bands of the visit order (rank thresholds): pass 0 grows
+      // geometrically for random orders and is cut into equal widths for the
+      // directional orders; refinement passes split their prefix evenly.
+      std::vector<int> bandEnds;
+      if (pass == 0) {
+        double size = randomOrder ? first : std::max<double>(first, std::ceil((double)end / kMaxBands));
+        double b = 0;
+        while (b < end && (int)bandEnds.size() < kMaxBands - 1) {
+          b = std::min<double>(end, b + std::max(1.0, size));
+          bandEnds.push_back((int)b);
+          if (randomOrder) size *= growth;
+        }
+        if (bandEnds.back() < (int)end) bandEnds.push_back((int)end);
+      } else {
+        for (unsigned r = 1; r <= refine; r++) bandEnds.push_back((int)((unsigned long long)end * r / refine));
+      }
+      const int nb = (int)bandEnds.size();
+      CK(cudaMemcpyAsync(dBandEnds, bandEnds.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
+      h2d += nb * sizeof(int);
+      // Bucket this pass's targets by (band, colour phase): targets of one
+      // phase are at least k apart, farther than a dense patch reaches, so
+      // the targets of one batch never read each other.
+      CK(rs_prep_batches(dTargets, (int)ntargets, (int)tw, (int)end, randomOrder ? 1 : 0, wa.seed ^ 0x5bd1e995u,
+                         dBandEnds, nb, k, work, batchStart, dPass, s));
+      launches += 4;
+      const int nbatches = nb * k * k;
+      wa.pass = (unsigned)pass;
+      wa.sparse = (pass == 0 && sparseOk) ? 1 : 0;
+      for (int b = 0; b < nbatches; b++) {
+        wa.batch = b;
+        if (opt.profile) prof.begin(s);
+        CK(rs_launch_wave(wa, (int)opt.warpsPerBlock, s));
+        if (opt.profile) prof.end(s);
+        CK(rs_launch_commit(wa, s));
+        launches += 2;
+      }
+      CK(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(st.hostInts + 3, batchStart + nbatches, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaEventRecord(epass, s));
+      wait_stream(st, epass, cancel);
+      if (hc.error) return fail(RESYNTH_ERROR_DEVICE, "wavefront kernel reported error %u", hc.error);
+      const unsigned visited = (unsigned)st.hostInts[3];
+      // callbacks the reference makes during this pass (lib/synthesize.h:493)
+      for (unsigned t = 0; t < end; t += 4096u) prog.tick();
+      const unsigned betters = hc.betters - bettersTotal;
+      bettersTotal = hc.betters;
+      stats.passes = pass + 1;
+      stats.passLength[pass] = visited;
+      stats.betters[pass] = betters;
+      if (*cancel || *st.abortHost) break;
+      if ((float)betters / ntargets < 0.1) break;
+    }
+    stats.visits = 0;
+    for (unsigned i = 0; i < stats.passes; i++) stats.visits += stats.passLength[i];
+    stats.evals = hc.evals;
+    stats.terms = hc.terms;
+    if (opt.profile) {
+      CK(cudaStreamSynchronize(s));
+      stats.waveMs = prof.total();
+      stats.waveLaunches = prof.count();
+      stats.waveTerms = hc.terms;
+    }
+  }
+  CK(rs_launch_unpack_colors(dT, (int)tw, (int)th, f.total_bpp, f.img_match_bpp, dp.tpx, s));
+  launches++;
+  CK(cudaEventRecord(e1, s));
+  if (opt.recordState) {
+    g_state.w = tw;
+    g_state.h = th;
+    g_state.src.resize((size_t)tw * th);
+    g_state.has.resize((size_t)tw * th);
+    CK(cudaMemcpyAsync(g_state.src.data(), dp.pb.src, g_state.src.size() * sizeof(int2), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(g_state.has.data(), dp.pb.has, g_state.has.size(), cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  stats.deviceMs = ms;
+  stats.launches += launches;
+  stats.h2dBytes += h2d;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(epass);
+  return 0;
+}
+
+// engine() core on host pixmaps.
+int run_engine_host(const TImageSynthParameters& p, const TFormatIndices& f, uint8_t* target, unsigned tw,
+                    unsigned th, const uint8_t* corpus, unsigned cw, unsigned ch, void (*cb)(int, void*), void* ctx,
+                    int* cancel, const TResynthOptions& opt, TResynthStats& stats) {
+  if (!supported_format(f)) return fail(RESYNTH_ERROR_UNSUPPORTED, "pixel layout not supported");
+  // All argument and data checks of the reference come before any device work
+  // (lib/engine.c:591-646), in the reference's order.
+  if (p.patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+  const bool devicePrep = opt.mode != RESYNTH_MODE_REPLAY && (p.matchContextType == 0 || p.matchContextType == 1);
+  HostPrep hp;
+  if (devicePrep) {
+    const size_t tn = (size_t)tw * th, cn = (size_t)cw * ch;
+    const int bpp = f.total_bpp;
+    bool anyTarget = false, anyCorpus = false;
+    for (size_t i = 0; i < tn && !anyTarget; i++) anyTarget = target[i * bpp] != 0;
+    if (!anyTarget) return IMAGE_SYNTH_ERROR_EMPTY_TARGET;
+    for (size_t i = 0; i < cn && !anyCorpus; i++)
+      anyCorpus = corpus[i * bpp] == 0xFF && (!f.isAlphaSource || corpus[i * bpp + f.alpha_bip] != 0);
+    if (!anyCorpus) return IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
+  } else {
+    const int prc = prepare(p, f, target, tw, th, corpus, cw, ch, hp);
+    if (prc) return prc;
+  }
+  Stream& st = thread_stream();
+  cudaStream_t s = st.s;
+  const size_t tb = (size_t)tw * th * f.total_bpp, cb_ = (size_t)cw * ch * f.total_bpp;
+  Arena ar(s);
+  uint8_t* dT = ar.alloc<uint8_t>(tb);
+  uint8_t* dC = ar.alloc<uint8_t>(cb_);
+  CK(cudaMemcpyAsync(dT, target, tb, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dC, corpus, cb_, cudaMemcpyHostToDevice, s));
+  stats.h2dBytes += tb + cb_;
+  const int rc = run_engine_device(p, f, dT, tw, th, dC, cw, ch, devicePrep ? nullptr : &hp, s, cb, ctx, cancel, opt,
+                                   stats);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(target, dT, tb, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  stats.d2hBytes += tb;
+  return 0;
+}
+
+int guarded(const char* what, const std::function<int()>& fn) {
+  try {
+    g_lastError.clear();
+    return fn();
+  } catch (const CudaError& e) {
+    return fail(RESYNTH_ERROR_DEVICE, "%s: %s (%s)", what, cudaGetErrorString(e.e), e.what);
+  } catch (const std::bad_alloc&) {
+    return fail(RESYNTH_ERROR_DEVICE, "%s: host out of memory", what);
+  }
+}
+
+TResynthOptions options_or_default(const TResynthOptions* o) {
+  TResynthOptions d;
+  resynthDefaultOptions(&d);
+  return o ? *o : d;
+}
+
+// Simple API adaption (lib/adaptSimple.h:47-354) and write-back.
+int image_synth_impl(ImageBuffer* img, ImageBuffer* mask, ImageBuffer* mask2, TImageFormat fmt,
+                     TImageSynthParameters* params, void (*cb)(int, void*), void* ctx, int* cancel,
+                     const TResynthOptions& opt, TResynthStats& stats) {
+  if (img->width != mask->width || img->height != mask->height) return IMAGE_SYNTH_ERROR_IMAGE_MASK_MISMATCH;
+  TImageSynthParameters defaults;
+  if (!params) {
+    setDefaultParams(&defaults);
+    params = &defaults;
+  }
+  TFormatIndices f;
+  const int rc0 = prepareImageFormatIndicesFromFormatType(&f, fmt);
+  if (rc0) return rc0;
+  const unsigned bpp = countPixelelsPerPixelForFormat(fmt), w = img->width, h = img->height;
+  const unsigned d = bpp + 1;
+  std::vector<uint8_t> tgt((size_t)w * h * d), cor((size_t)w * h * d);
+  ImageBuffer* cm = mask2 ? mask2 : mask;
+  for (unsigned y = 0; y < h; y++) {
+    const uint8_t* srow = img->data + y * img->rowBytes;
+    const uint8_t* mrow = mask->data + y * mask->rowBytes;
+    const uint8_t* crow = cm->data + y * cm->rowBytes;
+    for (unsigned x = 0; x < w; x++) {
+      uint8_t* t = &tgt[((size_t)y * w + x) * d];
+      uint8_t* c = &cor[((size_t)y * w + x) * d];
+      t[0] = mrow[x];
+      c[0] = mask2 ? crow[x] : (uint8_t)~crow[x];
+      memcpy(t + 1, srow + (size_t)x * bpp, bpp);
+      memcpy(c + 1, srow + (size_t)x * bpp, bpp);
+    }
+  }
+  int zero = 0;
+  if (!cancel) cancel = &zero;
+  const int rc = run_engine_host(*params, f, tgt.data(), w, h, cor.data(), w, h, cb, ctx, cancel, opt, stats);
+  if (!rc && !*cancel) {
+    for (unsigned y = 0; y < h; y++) {
+      uint8_t* drow = img->data + y * img->rowBytes;
+      for (unsigned x = 0; x < w; x++) memcpy(drow + (size_t)x * bpp, &tgt[((size_t)y * w + x) * d + 1], bpp);
+    }
+  }
+  return rc;
+}
+
+// Frozen-state scoring / energy on host buffers.
+int score_host(bool energyMode, const TImageSynthParameters* p, const TFormatIndices* f, const uint8_t* target,
+               unsigned tw, unsigned th, const uint8_t* corpus, unsigned cw, unsigned ch, const uint8_t* hasValue,
+               const Coordinates* sourceOf, const Coordinates* targets, unsigned n, const unsigned* candStart,
+               const Coordinates* cands, unsigned* outSum, Coordinates* outPt, unsigned* outCount,
+               unsigned long long* energy) {
+  if (!p || !f || !target || !corpus || !hasValue || !sourceOf || (!targets && n))
+    return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  if (p->patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+  if (!supported_format(*f)) return fail(RESYNTH_ERROR_UNSUPPORTED, "pixel layout not supported");
+  Stream& st = thread_stream();
+  cudaStream_t s = st.s;
+  Arena ar(s);
+  unsigned long long h2d = 0;
+  unsigned launches = 0;
+  const size_t tb = (size_t)tw * th * f->total_bpp, cbytes = (size_t)cw * ch * f->total_bpp;
+  const uint8_t* dT = ar.upload(target, tb, h2d);
+  const uint8_t* dC = ar.upload(corpus, cbytes, h2d);
+  const int mw = (int)std::min(tw, cw), mh = (int)std::min(th, ch);
+  const std::vector<int2>& offs = cached_offsets(mw, mh, LLONG_MAX);
+  DeviceProblem dp = make_problem(ar, s, *p, *f, dT, tw, th, dC, cw, ch, hasValue,
+                                  reinterpret_cast<const int2*>(sourceOf), offs, LLONG_MAX, h2d, launches);
+  rs::ScoreArgs sa{};
+  sa.pb = dp.pb;
+  sa.n = (int)n;
+  sa.targets = ar.upload(reinterpret_cast<const int2*>(targets), n, h2d);
+  sa.outSum = ar.alloc<unsigned>(n);
+  if (energyMode) {
+    sa.energy = ar.alloc<unsigned long long>(1);
+    CK(cudaMemsetAsync(sa.energy, 0, sizeof(unsigned long long), s));
+    CK(rs_launch_energy(sa, s));
+    unsigned long long e = 0;
+    CK(cudaMemcpyAsync(&e, sa.energy, sizeof e, cudaMemcpyDeviceToHost, s));
+    if (outSum) CK(cudaMemcpyAsync(outSum, sa.outSum, n * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *energy = e;
+    return 0;
+  }
+  if (!candStart || !outSum || !outPt) return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  const unsigned ncand = n ? candStart[n] : 0;
+  sa.candStart = ar.upload(candStart, (size_t)n + 1, h2d);
+  sa.cands = ar.upload(reinterpret_cast<const int2*>(cands), ncand, h2d);
+  sa.outPt = ar.alloc<int2>(n);
+  sa.outCount = ar.alloc<unsigned>(n);
+  if (n) CK(rs_launch_frozen(sa, s));
+  CK(cudaMemcpyAsync(outSum, sa.outSum, n * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(outPt, sa.outPt, n * sizeof(int2), cudaMemcpyDeviceToHost, s));
+  if (outCount) CK(cudaMemcpyAsync(outCount, sa.outCount, n * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // namespace
+
+// ====================================================== reference entry points
+
+RS_EXPORT void setDefaultParams(TImageSynthParameters* param) {
+  // lib/engineParams.c:8-19
+  param->isMakeSeamlesslyTileableHorizontally = 0;
+  param->isMakeSeamlesslyTileableVertically = 0;
+  param->matchContextType = 1;
+  param->mapWeight = 0.5;
+  param->sensitivityToOutliers = 0.117;
+  param->patchSize = 30;
+  param->maxProbeCount = 200;
+}
+
+RS_EXPORT unsigned int countPixelelsPerPixelForFormat(TImageFormat format) {
+  switch (format) {  // lib/imageFormat.c:39-56
+    case T_RGB: return 3;
+    case T_RGBA: return 4;
+    case T_Gray: return 1;
+    case T_GrayA: return 2;
+    default: return 0;
+  }
+}
+
+RS_EXPORT void prepareImageFormatIndices(TFormatIndices* indices, unsigned int colors, unsigned int mapColors,
+                                         int alphaT, int alphaS, int isMap) {
+  format_indices(indices, colors, mapColors, alphaT, alphaS, isMap);
+}
+
+RS_EXPORT int prepareImageFormatIndicesFromFormatType(TFormatIndices* indices, TImageFormat format) {
+  switch (format) {  // lib/imageFormat.c:65-113
+    case T_RGB: format_indices(indices, 3, 0, 0, 0, 0); return 0;
+    case T_RGBA: format_indices(indices, 3, 0, 1, 1, 0); return 0;
+    case T_Gray: format_indices(indices, 1, 0, 0, 0, 0); return 0;
+    case T_GrayA: format_indices(indices, 1, 0, 1, 1, 0); return 0;
+    default: return IMAGE_SYNTH_ERROR_INVALID_IMAGE_FORMAT;
+  }
+}
+
+RS_EXPORT void prepareDefaultFormatIndices(TFormatIndices* f) {
+  // lib/imageFormat.c:213-241: RGBA, internal pixel MRGBA
+  f->img_match_bpp = 3;
+  f->colorEndBip = 4;
+  f->alpha_bip = 4;
+  f->map_match_bpp = 0;
+  f->map_start_bip = 5;
+  f->map_end_bip = 5;
+  f->total_bpp = 5;
+  f->isAlphaTarget = 1;
+  f->isAlphaSource = 1;
+}
+
+// Maps: a GArray header followed by its storage (lib/mapOps.h:35-107).
+namespace {
+void map_alloc(Map* m, unsigned w, unsigned h, unsigned depth, size_t eltSize) {
+  m->width = w;
+  m->height = h;
+  m->depth = depth;
+  GArray* a = (GArray*)calloc(1, sizeof(GArray));
+  a->data = (char*)calloc((size_t)w * h ? (size_t)w * h : 1, eltSize);
+  a->len = 0;
+  m->data = a;
+}
+}  // namespace
+
+RS_EXPORT void free_map(Map* map) {
+  if (map->data) {
+    free(map->data->data);
+    free(map->data);
+  }
+  map->data = nullptr;
+}
+RS_EXPORT void new_pixmap(Map* map, unsigned int w, unsigned int h, unsigned int depth) {
+  map_alloc(map, w, h, depth, depth);
+}
+RS_EXPORT void new_bytemap(Map* map, unsigned int w, unsigned int h) { map_alloc(map, w, h, 1, 1); }
+RS_EXPORT void new_intmap(Map* map, unsigned int w, unsigned int h) {
+  map_alloc(map, w, h, sizeof(unsigned int), sizeof(unsigned int));
+}
+RS_EXPORT void new_coordmap(Map* map, unsigned int w, unsigned int h) {
+  map_alloc(map, w, h, sizeof(Coordinates), sizeof(Coordinates));
+}
+RS_EXPORT void set_bytemap(Map* map, unsigned char value) {
+  memset(map->data->data, value, (size_t)map->width * map->height);
+}
+RS_EXPORT void invert_bytemap(Map* map) {
+  unsigned char* d = (unsigned char*)map->data->data;
+  for (size_t i = 0, n = (size_t)map->width * map->height; i < n; i++) d[i] = (unsigned char)~d[i];
+}
+RS_EXPORT void interleave_mask(Map* pixmap, Map* mask) {
+  // lib/mapOps.h:153-168
+  const size_t n = (size_t)pixmap->width * pixmap->height;
+  unsigned char* p = (unsigned char*)pixmap->data->data;
+  const unsigned char* m = (const unsigned char*)mask->data->data;
+  for (size_t i = 0; i < n; i++) p[i * pixmap->depth] = m[i * mask->depth];
+}
+
+RS_EXPORT void resynthDefaultOptions(TResynthOptions* o) {
+  memset(o, 0, sizeof *o);
+  o->mode = default_mode();
+}
+
+RS_EXPORT int resynthSetMode(int mode) {
+  if (mode != RESYNTH_MODE_WAVEFRONT && mode != RESYNTH_MODE_REPLAY) return -1;
+  const int prev = default_mode();
+  g_defaultMode = mode;
+  return prev;
+}
+
+RS_EXPORT const char* resynthLastError(void) { return g_lastError.c_str(); }
+
+RS_EXPORT int engineEx(const TImageSynthParameters* parameters, const TFormatIndices* indices, Map* targetMap,
+                       Map* corpusMap, void (*cb)(int, void*), void* ctx, int* cancel,
+                       const TResynthOptions* options, TResynthStats* stats) {
+  if (!parameters || !indices || !targetMap || !corpusMap || !targetMap->data || !corpusMap->data)
+    return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  TResynthStats local{};
+  TResynthStats& st = stats ? *stats : local;
+  memset(&st, 0, sizeof st);
+  const auto t0 = std::chrono::steady_clock::now();
+  const TResynthOptions opt = options_or_default(options);
+  int zero = 0;
+  const int rc = guarded("engine", [&] {
+    return run_engine_host(*parameters, *indices, (uint8_t*)targetMap->data->data, targetMap->width,
+                           targetMap->height, (const uint8_t*)corpusMap->data->data, corpusMap->width,
+                           corpusMap->height, cb, ctx, cancel ? cancel : &zero, opt, st);
+  });
+  st.totalMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+RS_EXPORT int engine(TImageSynthParameters parameters, TFormatIndices* indices, Map* targetMap, Map* corpusMap,
+                     void (*cb)(int, void*), void* ctx, int* cancel) {
+  return engineEx(&parameters, indices, targetMap, corpusMap, cb, ctx, cancel, nullptr, nullptr);
+}
+
+RS_EXPORT int imageSynthEx(ImageBuffer* img, ImageBuffer* mask, ImageBuffer* mask2, TImageFormat fmt,
+                           TImageSynthParameters* params, void (*cb)(int, void*), void* ctx, int* cancel,
+                           const TResynthOptions* options, TResynthStats* stats) {
+  if (!img || !mask) return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  TResynthStats local{};
+  TResynthStats& st = stats ? *stats : local;
+  memset(&st, 0, sizeof st);
+  const auto t0 = std::chrono::steady_clock::now();
+  const TResynthOptions opt = options_or_default(options);
+  const int rc = guarded("imageSynth", [&] {
+    return image_synth_impl(img, mask, mask2, fmt, params, cb, ctx, cancel, opt, st);
+  });
+  st.totalMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+RS_EXPORT int imageSynth(ImageBuffer* img, ImageBuffer* mask, TImageFormat fmt, TImageSynthParameters* params,
+                         void (*cb)(int, void*), void* ctx, int* cancel) {
+  return imageSynthEx(img, mask, nullptr, fmt, params, cb, ctx, cancel, nullptr, nullptr);
+}
+
+RS_EXPORT int imageSynth2(ImageBuffer* img, ImageBuffer* mask, ImageBuffer* mask2, TImageFormat fmt,
+                          TImageSynthParameters* params, void (*cb)(int, void*), void* ctx, int* cancel) {
+  return imageSynthEx(img, mask, mask2, fmt, params, cb, ctx, cancel, nullptr, nullptr);
+}
+
+RS_EXPORT int engineDevice(const TImageSynthParameters* p, const TFormatIndices* f, unsigned char* dTarget,
+                           unsigned int tw, unsigned int th, const unsigned char* dCorpus, unsigned int cw,
+                           unsigned int ch, void* stream, void (*cb)(int, void*), void* ctx, int* cancel,
+                           const TResynthOptions* options, TResynthStats* stats) {
+  if (!p || !f || !dTarget || !dCorpus) return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  if (p->patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+  if (!supported_format(*f)) return fail(RESYNTH_ERROR_UNSUPPORTED, "pixel layout not supported");
+  TResynthStats local{};
+  TResynthStats& st = stats ? *stats : local;
+  memset(&st, 0, sizeof st);
+  const auto t0 = std::chrono::steady_clock::now();
+  const TResynthOptions opt = options_or_default(options);
+  const int rc = guarded("engineDevice", [&] {
+    return run_engine_device(*p, *f, dTarget, tw, th, dCorpus, cw, ch, nullptr, (cudaStream_t)stream, cb, ctx,
+                             cancel, opt, st);
+  });
+  st.totalMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return rc;
+}
+
+RS_EXPORT int resynthGetState(Coordinates* sourceOf, unsigned char* hasValue, unsigned int w, unsigned int h) {
+  if (g_state.w != w || g_state.h != h || g_state.src.empty())
+    return fail(RESYNTH_ERROR_ARGUMENT, "no recorded state of that size");
+  if (sourceOf) memcpy(sourceOf, g_state.src.data(), g_state.src.size() * sizeof(Coordinates));
+  if (hasValue) memcpy(hasValue, g_state.has.data(), g_state.has.size());
+  return 0;
+}
+
+RS_EXPORT int resynthFrozenBestFit(const TImageSynthParameters* p, const TFormatIndices* f, const unsigned char* target,
+                                   unsigned int tw, unsigned int th, const unsigned char* corpus, unsigned int cw,
+                                   unsigned int ch, const unsigned char* hasValue, const Coordinates* sourceOf,
+                                   const Coordinates* targets, unsigned int n, const unsigned int* candStart,
+                                   const Coordinates* cands, unsigned int* bestSum, Coordinates* bestPoint,
+                                   unsigned int* patchCount) {
+  return guarded("resynthFrozenBestFit", [&] {
+    return score_host(false, p, f, target, tw, th, corpus, cw, ch, hasValue, sourceOf, targets, n, candStart, cands,
+                      bestSum, bestPoint, patchCount, nullptr);
+  });
+}
+
+RS_EXPORT int resynthPatchEnergy(const TImageSynthParameters* p, const TFormatIndices* f, const unsigned char* target,
+                                 unsigned int tw, unsigned int th, const unsigned char* corpus, unsigned int cw,
+                                 unsigned int ch, const unsigned char* hasValue, const Coordinates* sourceOf,
+                                 const Coordinates* targets, unsigned int n, unsigned long long* energy,
+                                 unsigned int* perTarget) {
+  if (!energy) return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  return guarded("resynthPatchEnergy", [&] {
+    return score_host(true, p, f, target, tw, th, corpus, cw, ch, hasValue, sourceOf, targets, n, nullptr, nullptr,
+                      perTarget, nullptr, nullptr, energy);
+  });
+}

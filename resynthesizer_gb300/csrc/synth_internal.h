@@ -1,0 +1,114 @@
+// synth_internal.h -- structures shared by the host engine (synth_host.cpp)
+// and the CUDA kernels (synth_kernels.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rs {
+
+constexpr int kMaxNeighbors = 64;     // IMAGE_SYNTH_MAX_NEIGHBORS, lib/imageSynthConstants.h:26
+constexpr int kPasses = 6;            // MAX_PASSES, lib/passes.h:51
+constexpr int kTable = 512;           // metric table length, lib/matchWeighting.h:132-133
+
+// Device view of one synthesis problem.  Pixels are repacked into 32-bit
+// words: px = mask | c0 << 8 | c1 << 16 | c2 << 24 and map = m0 | m1 << 8 | m2 << 16.
+// Coordinates are int2 (x, y); a source of (-1, -1) means "none".
+struct Problem {
+  int tw, th;                 // target size
+  int cw, ch;                 // corpus size
+  int nc, nm;                 // colour and map channels matched (1..3, 0..3)
+  uint32_t* tpx;              // target pixels (tw*th)
+  uint32_t* tmap;             // target map channels (tw*th) or null
+  uint8_t* has;               // hasValue (tw*th)
+  int2* src;                  // sourceOf (tw*th)
+  const uint32_t* cpx;        // corpus pixels (cw*ch)
+  const uint32_t* cmap;       // corpus map channels (cw*ch) or null
+  const int2* cpts;           // corpus points (selected and not transparent)
+  int ncorpus;
+  const int2* offs;           // sorted offsets, offs[0] == (0, 0)
+  int noffs;
+  int patchLimit;             // the patch stops growing at max(patchSize, 2) neighbours
+  int tileH, tileV;
+  int boxW, boxH;             // offsets span |dx| < boxW, |dy| < boxH (the smaller image)
+  long long maxD2;            // offsets are cut at dx^2 + dy^2 <= maxD2
+  int fullCorpus;             // every corpus pixel is a corpus point: probes need no list
+  uint32_t clipCost;          // 65535 * nc + mapTable[0] * nm
+  const uint32_t* ctab;       // colour metric table (512 entries, widened to 32 bits)
+  const uint32_t* mtab;       // map metric table (512)
+};
+
+// Device counters accumulated by the synthesis kernels.
+struct Counters {
+  unsigned long long evals;
+  unsigned long long terms;
+  unsigned long long refEvals;   // replay: computeBestFit calls the reference would make
+  unsigned int betters;
+  unsigned int cursor;           // replay: position in the PRNG stream
+  unsigned int error;            // nonzero: a kernel gave up (bounded wait ran out)
+  unsigned int pad;
+};
+
+// Sequential replay of the reference order (one CTA).
+struct ReplayArgs {
+  Problem pb;
+  const int2* targets;           // targetPoints in the reference order
+  unsigned int* recentProber;    // cw*ch, init 0xFFFFFFFF
+  const int* randStream;         // libc rand() outputs after srand(1198472) and ordering
+  unsigned int randCount;
+  unsigned int trys;
+  Counters* ctr;
+};
+
+// One wavefront batch: targets[batchStart[batch] .. batchStart[batch + 1])
+// are synthesized together (the range lives in device memory, so batches can
+// be enqueued without a host round trip).
+struct WaveArgs {
+  Problem pb;
+  const int2* targets;           // this pass's targets, bucketed by batch
+  const int* batchStart;         // device: batch boundaries
+  int batch;
+  int sparse;                    // allowed: patches from the valued list targets[0 .. b0)
+  long long sparseLimit2;        // ... while b0 * b0 < sparseLimit2
+  unsigned int trys;
+  unsigned int seed, pass;
+  int2* stageSrc;                // per-batch-slot new source, (-2, -2) = unchanged
+  Counters* ctr;
+  const volatile int* abortFlag; // host-mapped; nonzero stops the batch
+};
+
+// Frozen-state scoring and energy.
+struct ScoreArgs {
+  Problem pb;
+  const int2* targets;
+  int n;
+  const unsigned int* candStart; // frozen: n+1 offsets into cands
+  const int2* cands;
+  unsigned int* outSum;
+  int2* outPt;
+  unsigned int* outCount;
+  unsigned long long* energy;    // energy mode: total
+};
+
+}  // namespace rs
+
+// Kernel launchers (synth_kernels.cu).  All return a cudaError_t.
+extern "C" {
+cudaError_t rs_launch_pack(const uint8_t* raw, int w, int h, int bpp, int colorStart, int nc, int mapStart,
+                           int nm, uint32_t* px, uint32_t* map, cudaStream_t s);
+cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc, const uint32_t* px,
+                                    cudaStream_t s);
+cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream_t s);
+cudaError_t rs_launch_wave(const rs::WaveArgs& a, int warpsPerBlock, cudaStream_t s);
+cudaError_t rs_launch_commit(const rs::WaveArgs& a, cudaStream_t s);
+cudaError_t rs_launch_frozen(const rs::ScoreArgs& a, cudaStream_t s);
+cudaError_t rs_launch_energy(const rs::ScoreArgs& a, cudaStream_t s);
+cudaError_t rs_prep_target(const uint8_t* raw, int w, int h, int bpp, int alpha, int hasAlpha, int useContext,
+                           uint8_t* has, int2* src, int* scratch, int2* targets, int* counts, cudaStream_t s);
+cudaError_t rs_prep_corpus(const uint8_t* raw, int w, int h, int bpp, int alpha, int hasAlpha, int* scratch,
+                           int2* points, int* count, cudaStream_t s);
+int rs_prep_scratch_ints(int w, int h);
+cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
+                            const int* dBandEnds, int nbands, int k, int* work, int* batchStart, int2* out,
+                            cudaStream_t s);
+}

@@ -1,0 +1,876 @@
+// synth_kernels.cu -- sm_103a kernels of the synthesis engine.
+//
+// Building blocks (each restating a reference routine):
+//   build_patch_*    prepare_neighbors, lib/synthesize.h:189-241
+//   term_cost        one neighbour term of computeBestFit, lib/synthesize.h:289-356
+//   score_warp       computeBestFit over an ordered candidate list with the
+//                    reference's result rule (strict-less update from UINT_MAX,
+//                    lib/synthesize.h:382-399), as a lexicographic minimum of
+//                    (patch sum, candidate index) -- early-out is exact because
+//                    every term is non-negative.
+// Kernels:
+//   k_replay   one CTA visiting targets in the reference order (bit-exact
+//              sequential replay of lib/synthesize.h:426-642)
+//   k_wave     warp-per-target synthesis of one wavefront batch
+//   k_commit   applies a batch's staged results (setColor/setSourceOf/setHasValue)
+//   k_frozen   frozen-state best fit over explicit candidate lists
+//   k_energy   full-patch metric at each target's source
+#include <climits>
+#include <cstdint>
+
+#include "synth_internal.h"
+
+namespace rs {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// One patch (TNeighbor[], lib/synthesize.h:120-125) as structure of arrays:
+// lanes that sit at different neighbours read different banks.
+struct Patch {
+  int off[kMaxNeighbors];        // (dy << 16) | (dx & 0xffff)
+  uint32_t px[kMaxNeighbors];    // target pixel word
+  uint32_t map[kMaxNeighbors];   // target map word
+  int2 src[kMaxNeighbors];       // sourceOf of the neighbour
+};
+
+__device__ __forceinline__ int pack_off(int dx, int dy) { return (int)((unsigned)dy << 16 | ((unsigned)dx & 0xffffu)); }
+__device__ __forceinline__ int off_dx(int o) { return (int)(short)(o & 0xffff); }
+__device__ __forceinline__ int off_dy(int o) { return o >> 16; }
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(kFull, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// lib/synthesize.h:81-113: wrap into the target when tiling, else clip.
+__device__ __forceinline__ bool wrap_or_clip(const Problem& pb, int& x, int& y) {
+  if (x < 0 || x >= pb.tw) {
+    if (!pb.tileH) return false;
+    x %= pb.tw;
+    if (x < 0) x += pb.tw;
+  }
+  if (y < 0 || y >= pb.th) {
+    if (!pb.tileV) return false;
+    y %= pb.th;
+    if (y < 0) y += pb.th;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void load_nb(const Problem& pb, Patch& P, int slot, int off, int qi) {
+  P.off[slot] = off;
+  P.src[slot] = pb.src[qi];
+  P.px[slot] = pb.tpx[qi];
+  P.map[slot] = pb.tmap ? pb.tmap[qi] : 0u;
+}
+
+// prepare_neighbors for one target with one warp: the target itself first,
+// then the nearest sorted offsets whose point lies in (or wraps into) the
+// target image and has a value, until the patch limit.  Returns the count.
+__device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int lane) {
+  if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
+  int count = 1;
+  const int limit = pb.patchLimit;
+  for (int base = 1; base < pb.noffs && count < limit; base += 32) {
+    const int j = base + lane;
+    bool ok = false;
+    int qi = 0;
+    int2 o = make_int2(0, 0);
+    if (j < pb.noffs) {
+      o = __ldg(&pb.offs[j]);
+      int qx = px + o.x, qy = py + o.y;
+      if (wrap_or_clip(pb, qx, qy)) {
+        qi = qy * pb.tw + qx;
+        ok = pb.has[qi] != 0;
+      }
+    }
+    const unsigned m = __ballot_sync(kFull, ok);
+    const int slot = count + __popc(m & lanemask_lt());
+    if (ok && slot < limit) load_nb(pb, P, slot, pack_off(o.x, o.y), qi);
+    count = min(limit, count + __popc(m));
+  }
+  __syncwarp();
+  return count;
+}
+
+// The same patch when the valued pixels are exactly list[0 .. V) and nothing
+// wraps: the nearest valued pixels in sorted-offset order (ascending
+// dx^2 + dy^2, ties by descending position in the offset box -- the order of
+// the offset list), selected by a warp-wide insertion into a sorted top list
+// instead of walking the offset list.  Much cheaper while V is small.
+__device__ int build_patch_sparse(const Problem& pb, int px, int py, Patch& P, unsigned long long* best,
+                                  const int2* list, int V, int lane) {
+  if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
+  const int lim = pb.patchLimit - 1;
+  const int bw = pb.boxW, bh = pb.boxH;
+  const unsigned W2 = 2u * bw - 1u;
+  int cnt = 0;
+  unsigned long long thr = ~0ull;
+  for (int base = 0; base < V; base += 32) {
+    const int j = base + lane;
+    unsigned long long key = ~0ull;
+    if (j < V) {
+      const int2 q = list[j];
+      const int dx = q.x - px, dy = q.y - py;
+      if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
+        const long long d2 = (long long)dx * dx + (long long)dy * dy;
+        if (d2 <= pb.maxD2) {
+          const unsigned idx = (unsigned)(dy + bh - 1) * W2 + (unsigned)(dx + bw - 1);
+          key = ((unsigned long long)d2 << 32) | (0xFFFFFFFFu - idx);
+        }
+      }
+    }
+    unsigned m = __ballot_sync(kFull, key < thr);
+    while (m) {
+      const int srcLane = __ffs(m) - 1;
+      m &= m - 1;
+      const unsigned long long k = __shfl_sync(kFull, key, srcLane);
+      if (k >= thr) continue;
+      const unsigned long long e0 = lane < cnt ? best[lane] : ~0ull;
+      const unsigned long long e1 = lane + 32 < cnt ? best[lane + 32] : ~0ull;
+      const int pos = __popc(__ballot_sync(kFull, e0 < k)) + __popc(__ballot_sync(kFull, e1 < k));
+      __syncwarp();
+      if (lane >= pos && lane < cnt && lane + 1 < lim) best[lane + 1] = e0;
+      if (lane + 32 >= pos && lane + 32 < cnt && lane + 33 < lim) best[lane + 33] = e1;
+      __syncwarp();
+      if (lane == 0) best[pos] = k;
+      __syncwarp();
+      cnt = min(cnt + 1, lim);
+      thr = cnt == lim ? best[lim - 1] : ~0ull;
+    }
+  }
+  for (int i = lane; i < cnt; i += 32) {
+    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
+    const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
+    load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
+  }
+  __syncwarp();
+  return 1 + cnt;
+}
+
+// One neighbour term of computeBestFit for candidate (cx, cy): the clip/mask
+// penalty, or the colour terms (skipped for the target itself) plus the map
+// terms.  Branch-free: an out-of-range point reads word 0 and is discarded.
+template <int NC, bool MAP>
+__device__ __forceinline__ uint32_t term_cost(const Problem& pb, const uint32_t* cpx, const uint32_t* cmap,
+                                              const uint32_t* ct, const uint32_t* mt, int cx, int cy, int off,
+                                              uint32_t t, uint32_t tm, bool self) {
+  const int qx = cx + off_dx(off), qy = cy + off_dy(off);
+  const bool inb = (unsigned)qx < (unsigned)pb.cw && (unsigned)qy < (unsigned)pb.ch;
+  const int qi = inb ? qy * pb.cw + qx : 0;
+  const uint32_t s = cpx[qi];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int c = 1; c <= NC; c++) sum += ct[256 + (int)((t >> (8 * c)) & 0xFFu) - (int)((s >> (8 * c)) & 0xFFu)];
+  if (self) sum = 0;
+  if (MAP) {
+    const uint32_t sm = cmap[qi];
+    for (int c = 0; c < pb.nm; c++) sum += mt[256 + (int)((tm >> (8 * c)) & 0xFFu) - (int)((sm >> (8 * c)) & 0xFFu)];
+  }
+  return (inb && (s & 0xFFu) == 0xFFu) ? sum : pb.clipCost;
+}
+
+// Full patch metric, one thread, stopping once the sum reaches stopAt.
+template <int NC, bool MAP>
+__device__ uint32_t patch_sum(const Problem& pb, const uint32_t* cpx, const uint32_t* cmap, const uint32_t* ct,
+                              const uint32_t* mt, int cx, int cy, const Patch& P, int n, uint32_t stopAt,
+                              unsigned& terms) {
+  uint32_t sum = 0;
+  for (int i = 0; i < n; i++) {
+    sum += term_cost<NC, MAP>(pb, cpx, cmap, ct, mt, cx, cy, P.off[i], P.px[i], MAP ? P.map[i] : 0u, i == 0);
+    terms++;
+    if (sum >= stopAt) break;
+  }
+  return sum;
+}
+
+// Scores candidates 0..ncand-1 (get(k) -> corpus point) against the patch
+// P[0..n) with one warp.  Each lane owns one candidate at a time and takes a
+// new one as soon as its current candidate is finished or can no longer win;
+// the result is the lexicographic minimum of (sum, k), i.e. the first strict
+// minimum in list order, exactly what a sequential computeBestFit loop keeps.
+// bestIdx == INT_MAX when ncand == 0.  Warp-uniform outputs.
+template <int NC, bool MAP, class Get>
+__device__ void score_warp(const Problem& pb, const uint32_t* cpx, const uint32_t* cmap, const uint32_t* ct,
+                           const uint32_t* mt, const Patch& P, int n, int ncand, Get get, int lane,
+                           uint32_t& bestVal, int& bestIdx, unsigned& terms, unsigned& evals) {
+  bestVal = 0xFFFFFFFFu;
+  bestIdx = INT_MAX;
+  int k = lane;
+  int2 c = make_int2(0, 0);
+  if (k < ncand) {
+    c = get(k);
+    evals++;
+  }
+  uint32_t sum = 0;
+  int i = 0;
+  int next = 32;
+  while (__any_sync(kFull, k < ncand)) {
+    const bool active = k < ncand;
+    if (active) {
+      uint32_t add = 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int ii = min(i + u, n - 1);
+        const uint32_t v = term_cost<NC, MAP>(pb, cpx, cmap, ct, mt, c.x, c.y, P.off[ii], P.px[ii],
+                                              MAP ? P.map[ii] : 0u, ii == 0);
+        add += (i + u < n) ? v : 0u;
+      }
+      const int step = min(4, n - i);
+      sum += add;
+      i += step;
+      terms += (unsigned)step;
+    }
+    const bool done = active && i >= n;
+    const bool fin = done && (sum < bestVal || (sum == bestVal && k < bestIdx));
+    if (__ballot_sync(kFull, fin)) {
+      unsigned long long key = fin ? ((unsigned long long)sum << 32) | (unsigned)k : ~0ull;
+      key = warp_min_u64(key);
+      const uint32_t kv = (uint32_t)(key >> 32);
+      const int ki = (int)(key & 0xffffffffu);
+      if (kv < bestVal || (kv == bestVal && ki < bestIdx)) {
+        bestVal = kv;
+        bestIdx = ki;
+      }
+    }
+    // A lane stops when finished or when its partial sum can no longer win
+    // (sums only grow; a tie wins only with the lower index).
+    const bool lost = active && !done && (sum > bestVal || (sum == bestVal && bestIdx < k));
+    const bool need = done || lost;
+    const unsigned nm = __ballot_sync(kFull, need);
+    if (need) {
+      k = next + __popc(nm & lanemask_lt());
+      // After a perfect match no later candidate can win.
+      if (bestVal == 0u) k = INT_MAX;
+      sum = 0;
+      i = 0;
+      if (k < ncand) {
+        c = get(k);
+        evals++;
+      }
+    }
+    next += __popc(nm);
+  }
+}
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x85ebca6bu;
+  x ^= x >> 13;
+  x *= 0xc2b2ae35u;
+  x ^= x >> 16;
+  return x;
+}
+
+// Counter-based probe draw (seed, pass, target pixel, probe) -> a uniform
+// corpus point: straight from the corpus rectangle when every pixel is a
+// corpus point, else through the corpus point list.
+__device__ __forceinline__ int2 probe_point(const Problem& pb, uint32_t seed, uint32_t pass, uint32_t pix,
+                                            uint32_t j) {
+  const uint32_t h = mix32(seed ^ mix32(pass * 0x9E3779B9u + 0x7f4a7c15u) ^ mix32(pix * 0x85EBCA77u + j * 0xC2B2AE3Du));
+  if (pb.fullCorpus) {
+    const uint32_t h2 = mix32(h + 0x632BE5ABu);
+    return make_int2((int)__umulhi(h, (uint32_t)pb.cw), (int)__umulhi(h2, (uint32_t)pb.ch));
+  }
+  return __ldg(&pb.cpts[__umulhi(h, (uint32_t)pb.ncorpus)]);
+}
+
+__device__ __forceinline__ bool corpus_ok(const Problem& pb, const uint32_t* cpx, int2 c) {
+  return (unsigned)c.x < (unsigned)pb.cw && (unsigned)c.y < (unsigned)pb.ch &&
+         (cpx[c.y * pb.cw + c.x] & 0xFFu) == 0xFFu;
+}
+
+// ----------------------------------------------------------- shared memory
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// Bulk (TMA) copy global -> shared, completion counted on an mbarrier.
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)));
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned phase) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Stages `words` 32-bit words (a multiple of 4, 16-byte aligned source) into
+// shared memory with bulk copies.  Returns false if the wait ran out.
+__device__ bool stage_words(uint32_t* dst, const uint32_t* src, unsigned words, uint64_t* bar) {
+  if (threadIdx.x == 0) {
+    mbar_init(bar);
+    mbar_expect_tx(bar, words * 4u);
+    const unsigned chunk = 16384;  // words per copy (64 KB)
+    for (unsigned w = 0; w < words; w += chunk) {
+      const unsigned cnt = min(chunk, words - w);
+      bulk_g2s(dst + w, src + w, cnt * 4u, bar);
+    }
+  }
+  __syncthreads();
+  bool ok = false;
+  for (int it = 0; it < (1 << 22); it++) {
+    if (mbar_try_wait(bar, 0)) {
+      ok = true;
+      break;
+    }
+    __nanosleep(64);
+  }
+  return ok;
+}
+
+// ------------------------------------------------------------------ frozen
+
+template <int NC, bool MAP>
+__global__ void __launch_bounds__(256) k_frozen(ScoreArgs a) {
+  __shared__ uint32_t ct[kTable], mt[kTable];
+  __shared__ Patch patches[8];
+  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
+    ct[i] = a.pb.ctab[i];
+    mt[i] = a.pb.mtab[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  Patch& P = patches[warp];
+  for (int t = blockIdx.x * (blockDim.x >> 5) + warp; t < a.n; t += nw) {
+    const int2 pos = a.targets[t];
+    const int n = build_patch_warp(a.pb, pos.x, pos.y, P, lane);
+    const unsigned c0 = a.candStart[t];
+    const int ncand = (int)(a.candStart[t + 1] - c0);
+    uint32_t bv;
+    int bi;
+    unsigned terms = 0, evals = 0;
+    score_warp<NC, MAP>(a.pb, a.pb.cpx, a.pb.cmap, ct, mt, P, n, ncand,
+                        [&](int k) { return a.cands[c0 + k]; }, lane, bv, bi, terms, evals);
+    if (lane == 0) {
+      a.outSum[t] = bv;
+      a.outPt[t] = bi == INT_MAX ? make_int2(-1, -1) : a.cands[c0 + bi];
+      a.outCount[t] = (unsigned)n;
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------ energy
+
+template <int NC, bool MAP>
+__global__ void __launch_bounds__(256) k_energy(ScoreArgs a) {
+  __shared__ uint32_t ct[kTable], mt[kTable];
+  __shared__ Patch patches[8];
+  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
+    ct[i] = a.pb.ctab[i];
+    mt[i] = a.pb.mtab[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  Patch& P = patches[warp];
+  unsigned long long acc = 0;
+  for (int t = blockIdx.x * (blockDim.x >> 5) + warp; t < a.n; t += nw) {
+    const int2 pos = a.targets[t];
+    const int n = build_patch_warp(a.pb, pos.x, pos.y, P, lane);
+    const int2 s = a.pb.src[pos.y * a.pb.tw + pos.x];
+    unsigned long long v = 0;
+    for (int i = lane; i < n; i += 32)
+      v += term_cost<NC, MAP>(a.pb, a.pb.cpx, a.pb.cmap, ct, mt, s.x, s.y, P.off[i], P.px[i], MAP ? P.map[i] : 0u,
+                              i == 0);
+    v = warp_sum_u64(v);
+    if (lane == 0) {
+      if (a.outSum) a.outSum[t] = (uint32_t)v;
+      acc += v;
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && acc) atomicAdd(a.energy, acc);
+}
+
+// ------------------------------------------------------------------ replay
+
+__device__ __forceinline__ unsigned long long block_min_u64(unsigned long long v, unsigned long long* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_min_u64(v);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  unsigned long long r = lane < nw ? red[lane] : ~0ull;
+  r = warp_min_u64(r);
+  __syncthreads();
+  return r;
+}
+
+// Visits targets[t0 .. t1) one after another, exactly as the single-threaded
+// reference (lib/synthesize.h:472-641), with the whole CTA working on each
+// visit: the patch scan, heuristic-1 candidates (continuations of the
+// neighbours' sources, minus those this target already probed, recorded in
+// recentProber), the random probes drawn from the reference's PRNG stream,
+// and the store.
+template <int NC, bool MAP>
+__global__ void __launch_bounds__(256, 1) k_replay(ReplayArgs a, int t0, int t1) {
+  __shared__ uint32_t ct[kTable], mt[kTable];
+  __shared__ Patch P;
+  __shared__ int2 hl[kMaxNeighbors];
+  __shared__ int2 rpt[256];
+  __shared__ unsigned long long red[8];
+  __shared__ int wcnt[8];
+  __shared__ int s_nh;
+  __shared__ unsigned s_cursor;
+  const Problem& pb = a.pb;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < kTable; i += blockDim.x) {
+    ct[i] = pb.ctab[i];
+    mt[i] = pb.mtab[i];
+  }
+  if (tid == 0) s_cursor = a.ctr->cursor;
+  __syncthreads();
+  unsigned cursor = s_cursor;
+  unsigned betters = 0, terms = 0;
+  unsigned long long refEvals = 0, evals = 0;
+  const unsigned div = 2147483647u / (unsigned)pb.ncorpus + 1u;   // lib/glibProxy.c:48
+
+  for (int t = t0; t < t1; t++) {
+    const int2 pos = a.targets[t];
+    const int pi = pos.y * pb.tw + pos.x;
+    // 1. patch (prepare_neighbors) with the whole block scanning offsets.
+    if (tid == 0) load_nb(pb, P, 0, 0, pi);
+    int count = 1;
+    for (int base = 1; base < pb.noffs && count < pb.patchLimit; base += blockDim.x) {
+      const int j = base + tid;
+      bool ok = false;
+      int qi = 0;
+      int2 o = make_int2(0, 0);
+      if (j < pb.noffs) {
+        o = pb.offs[j];
+        int qx = pos.x + o.x, qy = pos.y + o.y;
+        if (wrap_or_clip(pb, qx, qy)) {
+          qi = qy * pb.tw + qx;
+          ok = pb.has[qi] != 0;
+        }
+      }
+      const unsigned m = __ballot_sync(kFull, ok);
+      if (lane == 0) wcnt[warp] = __popc(m);
+      __syncthreads();
+      int before = 0, total = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        total += wcnt[w];
+        if (w < warp) before += wcnt[w];
+      }
+      const int slot = count + before + __popc(m & lanemask_lt());
+      if (ok && slot < pb.patchLimit) load_nb(pb, P, slot, pack_off(o.x, o.y), qi);
+      count = min(pb.patchLimit, count + total);
+      __syncthreads();
+    }
+    __syncthreads();
+    // 2. heuristic-1 list (warp 0): first occurrences, in neighbour order, of
+    //    in-corpus continuations not already probed by this target index.
+    if (warp == 0) {
+      int nh = 0;
+      for (int r = 0; r < count; r += 32) {
+        const int k = r + lane;
+        bool valid = false;
+        int2 c = make_int2(0, 0);
+        if (k < count && P.src[k].x != -1) {
+          c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
+          valid = corpus_ok(pb, pb.cpx, c) && a.recentProber[c.y * pb.cw + c.x] != (unsigned)t;
+        }
+        const unsigned long long key =
+            valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
+        const unsigned peers = __match_any_sync(kFull, key);
+        bool keep = valid && (peers & lanemask_lt()) == 0u;
+        for (int e = 0; e < nh && keep; e++)
+          if (hl[e].x == c.x && hl[e].y == c.y) keep = false;
+        const unsigned km = __ballot_sync(kFull, keep);
+        if (keep) hl[nh + __popc(km & lanemask_lt())] = c;
+        nh += __popc(km);
+        __syncwarp();
+      }
+      if (lane == 0) s_nh = nh;
+    }
+    __syncthreads();
+    const int nh = s_nh;
+    // 3. score heuristic-1 candidates (full sums) -> first strict minimum.
+    unsigned long long key = ~0ull;
+    if (tid < nh) {
+      const uint32_t s = patch_sum<NC, MAP>(pb, pb.cpx, pb.cmap, ct, mt, hl[tid].x, hl[tid].y, P, count,
+                                            0xFFFFFFFFu, terms);
+      key = ((unsigned long long)s << 32) | (unsigned)tid;
+    }
+    key = block_min_u64(key, red);
+    uint32_t bestVal = (uint32_t)(key >> 32);
+    int bestIdx = nh > 0 ? (int)(key & 0xffffffffu) : -1;
+    int2 bestPt = nh > 0 ? hl[bestIdx] : make_int2(0, 0);
+    const bool perfectH = nh > 0 && bestVal == 0u;
+    // recentProber is written for every evaluated candidate before a perfect one.
+    const int evaluatedH = perfectH ? bestIdx + 1 : nh;
+    if (tid < (perfectH ? bestIdx : nh)) a.recentProber[hl[tid].y * pb.cw + hl[tid].x] = (unsigned)t;
+    refEvals += (unsigned)evaluatedH;
+    evals += (unsigned)nh;
+    if (nh == 0) bestVal = 0xFFFFFFFFu;
+    // 4. random probes from the reference PRNG stream.
+    unsigned draws = 0;
+    if (!perfectH) {
+      for (unsigned j0 = 0; j0 < a.trys; j0 += blockDim.x) {
+        const unsigned j = j0 + tid;
+        unsigned long long rk = ~0ull;
+        if (j < a.trys) {
+          const unsigned pos_ = cursor + j;
+          const int r = pos_ < a.randCount ? a.randStream[pos_] : 0;
+          if (pos_ >= a.randCount) atomicOr(&a.ctr->error, 2u);
+          const int2 c = pb.cpts[(unsigned)r / div];
+          rpt[tid] = c;
+          const uint32_t s = patch_sum<NC, MAP>(pb, pb.cpx, pb.cmap, ct, mt, c.x, c.y, P, count, bestVal, terms);
+          evals++;
+          if (s < bestVal) rk = ((unsigned long long)s << 32) | j;
+        }
+        rk = block_min_u64(rk, red);
+        const unsigned chunkN = min((unsigned)blockDim.x, a.trys - j0);
+        if (rk != ~0ull) {
+          bestVal = (uint32_t)(rk >> 32);
+          bestPt = rpt[(unsigned)(rk & 0xffffffffu) - j0];
+          bestIdx = 1;
+        }
+        __syncthreads();  // rpt reuse
+        if (rk != ~0ull && bestVal == 0u) {
+          draws += (unsigned)(rk & 0xffffffffu) - j0 + 1u;
+          break;
+        }
+        draws += chunkN;
+      }
+    }
+    cursor += draws;
+    refEvals += draws;
+    // 5. store (only a better, different source), then setHasValue.
+    if (tid == 0) {
+      const bool bettered = nh > 0 || draws > 0;
+      const int2 cur = pb.src[pi];
+      if (bettered && (cur.x != bestPt.x || cur.y != bestPt.y)) {
+        betters++;
+        const uint32_t s = pb.cpx[bestPt.y * pb.cw + bestPt.x];
+        pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (s & 0xFFFFFF00u);
+        pb.src[pi] = bestPt;
+      }
+      pb.has[pi] = 1;
+    }
+    __syncthreads();
+  }
+  // statistics
+  unsigned long long tsum = warp_sum_u64(terms);
+  if (lane == 0) atomicAdd(&a.ctr->terms, tsum);
+  if (tid == 0) {
+    a.ctr->cursor = cursor;
+    a.ctr->betters += betters;
+    a.ctr->refEvals += refEvals;
+    a.ctr->evals += evals;
+  }
+}
+
+// --------------------------------------------------------------- wavefront
+
+struct WaveSmem {
+  static constexpr int kPerWarp =
+      (int)sizeof(Patch) + kMaxNeighbors * (int)sizeof(int2) + kMaxNeighbors * (int)sizeof(unsigned long long);
+};
+
+// One wavefront batch: a warp per target.  Candidates are the deduplicated
+// in-corpus continuations of the patch's sources followed by `trys`
+// counter-based random probes; the best (first strict minimum) different
+// source is staged for k_commit.
+template <int NC, bool MAP, bool SMEMC>
+__global__ void __launch_bounds__(512, 1) k_wave(WaveArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int b0 = a.batchStart[a.batch], b1 = a.batchStart[a.batch + 1];
+  const int nslots = b1 - b0;
+  // CTAs beyond this batch's size leave before staging anything.
+  if ((int)(blockIdx.x * (blockDim.x >> 5)) >= nslots) return;
+  uint32_t* ct = reinterpret_cast<uint32_t*>(smem);
+  uint32_t* mt = ct + kTable;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(mt + kTable);
+  unsigned char* p = smem + 2 * kTable * 4 + 16;
+  const Problem& pb = a.pb;
+  const uint32_t* cpx = pb.cpx;
+  const uint32_t* cmap = pb.cmap;
+  const unsigned cwords = ((unsigned)(pb.cw * pb.ch) + 3u) & ~3u;
+  if (SMEMC) {
+    uint32_t* scpx = reinterpret_cast<uint32_t*>(p);
+    p += cwords * 4;
+    uint32_t* scmap = nullptr;
+    if (MAP) {
+      scmap = reinterpret_cast<uint32_t*>(p);
+      p += cwords * 4;
+    }
+    bool ok = stage_words(scpx, pb.cpx, cwords, bar);
+    if (MAP && ok) ok = stage_words(scmap, pb.cmap, cwords, bar + 1);
+    if (!ok) {
+      if (threadIdx.x == 0) atomicOr(&a.ctr->error, 1u);
+      return;
+    }
+    cpx = scpx;
+    cmap = scmap;
+  }
+  __shared__ int s_abort;
+  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
+    ct[i] = pb.ctab[i];
+    mt[i] = pb.mtab[i];
+  }
+  // One read of the host-mapped flag per CTA, so the whole CTA agrees.
+  if (threadIdx.x == 0) s_abort = *a.abortFlag;
+  __syncthreads();
+  if (s_abort) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* wbase = p + warp * WaveSmem::kPerWarp;
+  Patch& P = *reinterpret_cast<Patch*>(wbase);
+  int2* prop = reinterpret_cast<int2*>(wbase + sizeof(Patch));
+  unsigned long long* topk = reinterpret_cast<unsigned long long*>(wbase + sizeof(Patch) + kMaxNeighbors * sizeof(int2));
+  const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  unsigned terms = 0, evals = 0;
+  for (int slot = blockIdx.x * (blockDim.x >> 5) + warp; slot < nslots; slot += nw) {
+    const int t = b0 + slot;
+    const int2 pos = a.targets[t];
+    const int pi = pos.y * pb.tw + pos.x;
+    const int n = sparse ? build_patch_sparse(pb, pos.x, pos.y, P, topk, a.targets, b0, lane)
+                         : build_patch_warp(pb, pos.x, pos.y, P, lane);
+    // continuation candidates, deduplicated, in neighbour order
+    int np = 0;
+    for (int r = 0; r < n; r += 32) {
+      const int k = r + lane;
+      bool valid = false;
+      int2 c = make_int2(0, 0);
+      if (k < n && P.src[k].x >= 0) {
+        c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
+        valid = corpus_ok(pb, cpx, c);
+      }
+      const unsigned long long key =
+          valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
+      const unsigned peers = __match_any_sync(kFull, key);
+      bool keep = valid && (peers & lanemask_lt()) == 0u;
+      for (int e = 0; e < np && keep; e++)
+        if (prop[e].x == c.x && prop[e].y == c.y) keep = false;
+      const unsigned km = __ballot_sync(kFull, keep);
+      if (keep) prop[np + __popc(km & lanemask_lt())] = c;
+      np += __popc(km);
+      __syncwarp();
+    }
+    const int ncand = np + (int)a.trys;
+    uint32_t bv;
+    int bi;
+    score_warp<NC, MAP>(
+        pb, cpx, cmap, ct, mt, P, n, ncand,
+        [&](int k) { return k < np ? prop[k] : probe_point(pb, a.seed, a.pass, (uint32_t)pi, (uint32_t)(k - np)); },
+        lane, bv, bi, terms, evals);
+    if (lane == 0) {
+      int2 out = make_int2(-2, -2);
+      if (bi != INT_MAX) {
+        const int2 best = bi < np ? prop[bi] : probe_point(pb, a.seed, a.pass, (uint32_t)pi, (uint32_t)(bi - np));
+        const int2 cur = pb.src[pi];
+        if (cur.x != best.x || cur.y != best.y) out = best;
+      }
+      a.stageSrc[slot] = out;
+    }
+    __syncwarp();
+  }
+  unsigned long long tv = warp_sum_u64(terms), ev = warp_sum_u64(evals);
+  if (lane == 0) {
+    atomicAdd(&a.ctr->terms, tv);
+    atomicAdd(&a.ctr->evals, ev);
+  }
+}
+
+__global__ void k_commit(WaveArgs a) {
+  const Problem& pb = a.pb;
+  // An aborted batch may be partly staged: apply none of it (one read per CTA).
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = *a.abortFlag;
+  __syncthreads();
+  const int b0 = a.batchStart[a.batch];
+  const int nslots = s_abort ? 0 : a.batchStart[a.batch + 1] - b0;
+  unsigned better = 0;
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nslots; slot += gridDim.x * blockDim.x) {
+    const int2 pos = a.targets[b0 + slot];
+    const int pi = pos.y * pb.tw + pos.x;
+    const int2 s = a.stageSrc[slot];
+    if (s.x != -2) {
+      const uint32_t c = pb.cpx[s.y * pb.cw + s.x];
+      pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (c & 0xFFFFFF00u);
+      pb.src[pi] = s;
+      better++;
+    }
+    pb.has[pi] = 1;
+  }
+  for (int o = 16; o > 0; o >>= 1) better += __shfl_xor_sync(kFull, better, o);
+  if ((threadIdx.x & 31) == 0 && better) atomicAdd(&a.ctr->betters, better);
+}
+
+// ---------------------------------------------------------- pack / unpack
+
+__global__ void k_pack(const uint8_t* raw, int npx, int bpp, int colorStart, int nc, int mapStart, int nm,
+                       uint32_t* px, uint32_t* map) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x) {
+    const uint8_t* q = raw + (size_t)i * bpp;
+    uint32_t w = q[0];
+    for (int c = 0; c < nc; c++) w |= (uint32_t)q[colorStart + c] << (8 * (c + 1));
+    px[i] = w;
+    if (map) {
+      uint32_t m = 0;
+      for (int c = 0; c < nm; c++) m |= (uint32_t)q[mapStart + c] << (8 * c);
+      map[i] = m;
+    }
+  }
+}
+
+__global__ void k_unpack_colors(uint8_t* raw, int npx, int bpp, int nc, const uint32_t* px) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x) {
+    uint8_t* q = raw + (size_t)i * bpp;
+    const uint32_t w = px[i];
+    for (int c = 0; c < nc; c++) q[1 + c] = (uint8_t)(w >> (8 * (c + 1)));
+  }
+}
+
+int grid_for(int n, int perBlock, int maxBlocks) {
+  int g = (n + perBlock - 1) / perBlock;
+  return g < 1 ? 1 : (g > maxBlocks ? maxBlocks : g);
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+}  // namespace
+}  // namespace rs
+
+using namespace rs;
+
+#define RS_DISPATCH(NCV, MAPV, CALL)                                       \
+  do {                                                                     \
+    if ((NCV) == 1) {                                                      \
+      if (MAPV) { constexpr int NC = 1; constexpr bool MAP = true; CALL; } \
+      else { constexpr int NC = 1; constexpr bool MAP = false; CALL; }     \
+    } else if ((NCV) == 2) {                                               \
+      if (MAPV) { constexpr int NC = 2; constexpr bool MAP = true; CALL; } \
+      else { constexpr int NC = 2; constexpr bool MAP = false; CALL; }     \
+    } else {                                                               \
+      if (MAPV) { constexpr int NC = 3; constexpr bool MAP = true; CALL; } \
+      else { constexpr int NC = 3; constexpr bool MAP = false; CALL; }     \
+    }                                                                      \
+  } while (0)
+
+extern "C" cudaError_t rs_launch_pack(const uint8_t* raw, int w, int h, int bpp, int colorStart, int nc,
+                                      int mapStart, int nm, uint32_t* px, uint32_t* map, cudaStream_t s) {
+  const int n = w * h;
+  k_pack<<<grid_for(n, 256, sm_count() * 8), 256, 0, s>>>(raw, n, bpp, colorStart, nc, mapStart, nm, px, map);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc, const uint32_t* px,
+                                               cudaStream_t s) {
+  const int n = w * h;
+  k_unpack_colors<<<grid_for(n, 256, sm_count() * 8), 256, 0, s>>>(raw, n, bpp, nc, px);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_launch_replay(const ReplayArgs& a, int t0, int t1, cudaStream_t s) {
+  RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (k_replay<NC, MAP><<<1, 256, 0, s>>>(a, t0, t1)));
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_launch_frozen(const ScoreArgs& a, cudaStream_t s) {
+  RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (k_frozen<NC, MAP><<<grid_for(a.n, 8, sm_count() * 8), 256, 0, s>>>(a)));
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_launch_energy(const ScoreArgs& a, cudaStream_t s) {
+  RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (k_energy<NC, MAP><<<grid_for(a.n, 8, sm_count() * 8), 256, 0, s>>>(a)));
+  return cudaGetLastError();
+}
+
+namespace {
+size_t wave_smem(const Problem& pb, bool smemc, int warps) {
+  size_t b = 2 * kTable * 4 + 16;
+  if (smemc) {
+    const size_t cwords = ((size_t)pb.cw * pb.ch + 3) & ~(size_t)3;
+    b += cwords * 4 * (pb.nm > 0 ? 2 : 1);
+  }
+  return b + (size_t)warps * WaveSmem::kPerWarp;
+}
+
+template <int NC, bool MAP, bool SMEMC>
+cudaError_t launch_wave_t(const WaveArgs& a, int warps, size_t smem, cudaStream_t s) {
+  auto kern = k_wave<NC, MAP, SMEMC>;
+  static size_t configured = 0;
+  if (smem > configured) {
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = smem;
+  }
+  static int perSm = 0;
+  static size_t perSmFor = 0;
+  if (perSmFor != smem) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
+    perSmFor = smem;
+  }
+  if (perSm < 1) return cudaErrorInvalidConfiguration;
+  // Persistent grid: the batch size is only known on the device.
+  kern<<<sm_count() * perSm, warps * 32, smem, s>>>(a);
+  return cudaGetLastError();
+}
+}  // namespace
+
+extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, cudaStream_t s) {
+  if (warps < 1) warps = 16;
+  if (warps > 16) warps = 16;
+  const size_t smemCorpus = wave_smem(a.pb, true, warps);
+  const bool smemc = smemCorpus <= 110 * 1024;
+  const size_t smem = smemc ? smemCorpus : wave_smem(a.pb, false, warps);
+  cudaError_t e = cudaSuccess;
+  if (smemc) {
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, true>(a, warps, smem, s)));
+  } else {
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, false>(a, warps, smem, s)));
+  }
+  return e;
+}
+
+extern "C" cudaError_t rs_launch_commit(const WaveArgs& a, cudaStream_t s) {
+  k_commit<<<sm_count() * 2, 256, 0, s>>>(a);
+  return cudaGetLastError();
+}

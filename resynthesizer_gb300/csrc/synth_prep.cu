@@ -1,0 +1,234 @@
+// synth_prep.cu -- device-side preparation for the wavefront mode.
+//
+// The reference prepares on the host (lib/engine.c:338-431): the selected
+// target points in row-major order with their initial hasValue, and the
+// corpus points (mask == 0xFF and not transparent).  Here the same lists are
+// built by deterministic stream compaction, and each pass's targets are
+// bucketed by (band, colour phase) with a counting sort so that batch b is
+// targets[batchStart[b] .. batchStart[b+1]).
+#include <algorithm>
+#include <cstdint>
+
+#include "synth_internal.h"
+
+namespace rs {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 16;
+constexpr int kChunk = kThreads * kItems;   // pixels per block in the compactions
+
+__device__ __forceinline__ uint32_t mix32p(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x85ebca6bu;
+  x ^= x >> 13;
+  x *= 0xc2b2ae35u;
+  x ^= x >> 16;
+  return x;
+}
+
+// Predicates on the interleaved pixmap.
+struct PixPred {
+  const uint8_t* raw;
+  int bpp, alpha, hasAlpha;
+  int mode;   // 0: target selected (mask != 0), 1: corpus point (mask == 0xFF and opaque)
+  __device__ bool operator()(int i) const {
+    const uint8_t* q = raw + (size_t)i * bpp;
+    if (mode == 0) return q[0] != 0;
+    return q[0] == 0xFF && (!hasAlpha || q[alpha] != 0);
+  }
+};
+
+// Block-wide exclusive scan of one count per thread (kThreads threads).
+__device__ int block_exclusive(int v, int* warpSums, int& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warpSums[warp] = x;
+  __syncthreads();
+  int before = 0;
+  total = 0;
+  for (int w = 0; w < kThreads / 32; w++) {
+    if (w < warp) before += warpSums[w];
+    total += warpSums[w];
+  }
+  __syncthreads();
+  return before + x - v;
+}
+
+// Target init: hasValue = useContext && !selected && opaque (lib/engine.c:366-384),
+// sourceOf = (-1, -1); per-block counts of selected pixels; flags whether any
+// pixel has a value (context).
+__global__ void k_init_target(const uint8_t* raw, int npx, int bpp, int alpha, int hasAlpha, int useContext,
+                              uint8_t* has, int2* src, int* blockCounts, int* anyContext) {
+  const int base = blockIdx.x * kChunk;
+  int cnt = 0, ctx = 0;
+  for (int k = 0; k < kItems; k++) {
+    const int i = base + k * kThreads + threadIdx.x;
+    if (i < npx) {
+      const uint8_t* q = raw + (size_t)i * bpp;
+      const bool sel = q[0] != 0;
+      const bool opaque = !hasAlpha || q[alpha] != 0;
+      const uint8_t hv = (useContext && !sel && opaque) ? 1 : 0;
+      has[i] = hv;
+      src[i] = make_int2(-1, -1);
+      cnt += sel;
+      ctx |= hv;
+    }
+  }
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
+  ctx = __reduce_or_sync(0xffffffffu, ctx);
+  __shared__ int s[kThreads / 32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+  if ((threadIdx.x & 31) == 0 && ctx) atomicOr(anyContext, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kThreads / 32; w++) t += s[w];
+    blockCounts[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_count(PixPred pred, int npx, int* blockCounts) {
+  const int base = blockIdx.x * kChunk;
+  int cnt = 0;
+  for (int k = 0; k < kItems; k++) {
+    const int i = base + k * kThreads + threadIdx.x;
+    if (i < npx && pred(i)) cnt++;
+  }
+  cnt = __reduce_add_sync(0xffffffffu, cnt);
+  __shared__ int s[kThreads / 32];
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kThreads / 32; w++) t += s[w];
+    blockCounts[blockIdx.x] = t;
+  }
+}
+
+// Exclusive scan of n counts by one block; offsets[n] = total.
+__global__ void k_scan(const int* counts, int n, int* offsets) {
+  __shared__ int warpSums[kThreads / 32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int b = 0; b < n; b += kThreads) {
+    const int i = b + threadIdx.x;
+    const int v = i < n ? counts[i] : 0;
+    int total;
+    const int ex = block_exclusive(v, warpSums, total);
+    if (i < n) offsets[i] = carry + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) offsets[n] = carry;
+}
+
+// Writes the (x, y) of every pixel satisfying pred, in row-major order.
+__global__ void k_compact(PixPred pred, int npx, int w, const int* blockOffsets, int2* out) {
+  __shared__ int warpSums[kThreads / 32];
+  int pos = blockOffsets[blockIdx.x];
+  const int base = blockIdx.x * kChunk;
+  for (int k = 0; k < kItems; k++) {
+    const int i = base + k * kThreads + threadIdx.x;
+    const bool f = i < npx && pred(i);
+    int total;
+    const int ex = block_exclusive(f ? 1 : 0, warpSums, total);
+    if (f) out[pos + ex] = make_int2(i % w, i / w);
+    pos += total;
+  }
+}
+
+// Batch keys of one pass.  rank = position in the visit order: given (the
+// host order) or drawn from a hash of the pixel (random orders).  Targets of
+// rank >= endRank are not visited this pass.  key = band * K + phase.
+__global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
+                             const int* bandEnds, int nbands, int k, int* keys, int* hist) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int2 p = targets[t];
+    const int rank = randomOrder ? (int)__umulhi(mix32p((uint32_t)(p.y * tw + p.x) * 0x9E3779B1u ^ seed), (uint32_t)n)
+                                 : t;
+    int key = -1;
+    if (rank < endRank) {
+      int band = 0;
+      while (band < nbands - 1 && rank >= bandEnds[band]) band++;
+      key = band * k * k + (p.y % k) * k + (p.x % k);
+      atomicAdd(&hist[key], 1);
+    }
+    keys[t] = key;
+  }
+}
+
+__global__ void k_scatter(const int2* targets, int n, const int* keys, int* cursor, int2* out) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int key = keys[t];
+    if (key >= 0) out[atomicAdd(&cursor[key], 1)] = targets[t];
+  }
+}
+
+__global__ void k_copy_int(const int* a, int* b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
+}
+
+int blocks_for(int n, int per) { return (n + per - 1) / per; }
+
+}  // namespace
+}  // namespace rs
+
+using namespace rs;
+
+extern "C" cudaError_t rs_prep_target(const uint8_t* raw, int w, int h, int bpp, int alpha, int hasAlpha,
+                                      int useContext, uint8_t* has, int2* src, int* scratch, int2* targets,
+                                      int* counts, cudaStream_t s) {
+  // scratch: 2 * nblocks + 1 ints; counts[0] = number of targets, counts[1] = any context
+  const int npx = w * h, nb = blocks_for(npx, kChunk);
+  int* blockCounts = scratch;
+  int* offsets = scratch + nb;
+  cudaMemsetAsync(counts + 1, 0, sizeof(int), s);
+  k_init_target<<<nb, kThreads, 0, s>>>(raw, npx, bpp, alpha, hasAlpha, useContext, has, src, blockCounts, counts + 1);
+  k_scan<<<1, kThreads, 0, s>>>(blockCounts, nb, offsets);
+  PixPred pred{raw, bpp, alpha, hasAlpha, 0};
+  k_compact<<<nb, kThreads, 0, s>>>(pred, npx, w, offsets, targets);
+  cudaMemcpyAsync(counts, offsets + nb, sizeof(int), cudaMemcpyDeviceToDevice, s);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_prep_corpus(const uint8_t* raw, int w, int h, int bpp, int alpha, int hasAlpha,
+                                      int* scratch, int2* points, int* count, cudaStream_t s) {
+  const int npx = w * h, nb = blocks_for(npx, kChunk);
+  int* blockCounts = scratch;
+  int* offsets = scratch + nb;
+  PixPred pred{raw, bpp, alpha, hasAlpha, 1};
+  k_count<<<nb, kThreads, 0, s>>>(pred, npx, blockCounts);
+  k_scan<<<1, kThreads, 0, s>>>(blockCounts, nb, offsets);
+  k_compact<<<nb, kThreads, 0, s>>>(pred, npx, w, offsets, points);
+  cudaMemcpyAsync(count, offsets + nb, sizeof(int), cudaMemcpyDeviceToDevice, s);
+  return cudaGetLastError();
+}
+
+extern "C" int rs_prep_scratch_ints(int w, int h) { return 2 * blocks_for(w * h, kChunk) + 1; }
+
+// Buckets the targets of one pass into batches: out[batchStart[b] ..
+// batchStart[b+1]) are the targets of batch b = band * k * k + phase.
+// work: 3 * nkeys + 1 + n ints.
+extern "C" cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder,
+                                       uint32_t seed, const int* dBandEnds, int nbands, int k, int* work,
+                                       int* batchStart, int2* out, cudaStream_t s) {
+  const int nkeys = nbands * k * k;
+  int* hist = work;
+  int* cursor = work + nkeys;
+  int* keys = work + 2 * nkeys + 1;
+  cudaMemsetAsync(hist, 0, sizeof(int) * nkeys, s);
+  const int g = std::min(blocks_for(n, 256), 1184);
+  k_batch_keys<<<g, 256, 0, s>>>(targets, n, tw, endRank, randomOrder, seed, dBandEnds, nbands, k, keys, hist);
+  k_scan<<<1, kThreads, 0, s>>>(hist, nkeys, batchStart);
+  k_copy_int<<<blocks_for(nkeys, 256), 256, 0, s>>>(batchStart, cursor, nkeys);
+  k_scatter<<<g, 256, 0, s>>>(targets, n, keys, cursor, out);
+  return cudaGetLastError();
+}
