@@ -225,6 +225,34 @@ int resynthPatchEnergy(const TImageSynthParameters *parameters, const TFormatInd
                        const Coordinates *targets, unsigned int targetCount,
                        unsigned long long *energy, unsigned int *perTarget);
 
+/* No counterpart in the reference.  Frozen-state best fit, as
+ * resynthFrozenBestFit, for callers that cannot let a library allocate device
+ * memory -- a host application that reserves the GPU's memory up front and
+ * hands out every buffer from its own pool, or a latency-critical loop that
+ * cannot afford cudaMalloc's implicit device-wide synchronisation.
+ *   - Every pointer is device memory owned by the caller, with the same
+ *     meaning as in resynthFrozenBestFit; the call allocates nothing.
+ *   - Working memory is one 8 MiB array inside the library, held by every GPU
+ *     that loads the library until the process exits.  The images must fit:
+ *     4 KiB + 4 * (targetWidth*targetHeight + corpusWidth*corpusHeight rounded
+ *     up to 4) bytes, doubled when map channels are matched; larger images
+ *     return RESYNTH_ERROR_UNSUPPORTED with the reason in resynthLastError().
+ *   - Work is enqueued on `stream` (a cudaStream_t, NULL = the default stream)
+ *     and the outputs are ready when the stream reaches that point.
+ *   - All calls share the one working array: calls that may overlap on the GPU
+ *     (on different streams without ordering between them) race and corrupt
+ *     each other's results.  Every call rewrites everything it reads there.
+ *   - The first call on each device looks up the array's device address with
+ *     that device current; make that first call before any stream capture. */
+int resynthFrozenBestFitNoAlloc(const TImageSynthParameters *parameters, const TFormatIndices *indices,
+                                const unsigned char *dTarget, unsigned int targetWidth, unsigned int targetHeight,
+                                const unsigned char *dCorpus, unsigned int corpusWidth, unsigned int corpusHeight,
+                                const unsigned char *dHasValue, const Coordinates *dSourceOf,
+                                const Coordinates *dTargets, unsigned int targetCount,
+                                const unsigned int *dCandStart, const Coordinates *dCandidates,
+                                unsigned int *dBestSum, Coordinates *dBestPoint, unsigned int *dPatchCount,
+                                void *stream);
+
 /* Text of the last error on this thread ("" if none). */
 const char *resynthLastError(void);
 

@@ -38,16 +38,15 @@ namespace {
 
 // ------------------------------------------------------------------ errors
 
-thread_local std::string g_lastError;
+// Fixed buffer: reporting an error never allocates.
+thread_local char g_lastError[512];
 
 int fail(int code, const char* fmt, ...) {
-  char buf[512];
   va_list ap;
   va_start(ap, fmt);
-  vsnprintf(buf, sizeof buf, fmt, ap);
+  vsnprintf(g_lastError, sizeof g_lastError, fmt, ap);
   va_end(ap);
-  g_lastError = buf;
-  if (code == RESYNTH_ERROR_DEVICE) fprintf(stderr, "resynthesizer: %s\n", buf);
+  if (code == RESYNTH_ERROR_DEVICE) fprintf(stderr, "resynthesizer: %s\n", g_lastError);
   return code;
 }
 
@@ -839,7 +838,7 @@ int run_engine_host(const TImageSynthParameters& p, const TFormatIndices& f, uin
 
 int guarded(const char* what, const std::function<int()>& fn) {
   try {
-    g_lastError.clear();
+    g_lastError[0] = 0;
     return fn();
   } catch (const CudaError& e) {
     return fail(RESYNTH_ERROR_DEVICE, "%s: %s (%s)", what, cudaGetErrorString(e.e), e.what);
@@ -1058,7 +1057,13 @@ RS_EXPORT int resynthSetMode(int mode) {
   return prev;
 }
 
-RS_EXPORT const char* resynthLastError(void) { return g_lastError.c_str(); }
+RS_EXPORT const char* resynthLastError(void) { return g_lastError; }
+
+// Internal helpers for the other translation units.
+extern "C" int rs_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+extern "C" void rs_metric_tables(double sensitivity, double mapWeight, uint32_t* ct, uint32_t* mt) {
+  metric_tables(sensitivity, mapWeight, ct, mt);
+}
 
 RS_EXPORT int engineEx(const TImageSynthParameters* parameters, const TFormatIndices* indices, Map* targetMap,
                        Map* corpusMap, void (*cb)(int, void*), void* ctx, int* cancel,

@@ -874,3 +874,234 @@ extern "C" cudaError_t rs_launch_commit(const WaveArgs& a, cudaStream_t s) {
   k_commit<<<sm_count() * 2, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
+
+// ====================================================================
+// Frozen-state best fit without device allocation.
+//
+// Some callers cannot let a library call cudaMalloc: a host application that
+// reserves the GPU's memory up front and hands out every buffer from its own
+// pool, or a latency-critical loop that cannot afford cudaMalloc's implicit
+// device-wide synchronisation.  resynthFrozenBestFitNoAlloc serves them: the
+// caller passes device buffers for every input and output, and the working
+// memory (packed pixel words and metric tables) lives in the file-scope
+// array below, which every GPU that loads this library holds until exit.
+// Patches are built by scanning square rings of offsets around the target
+// instead of walking a sorted offset list, so no list has to be stored.
+// ====================================================================
+
+#include <mutex>
+
+#include "../../include/resynthesizer.h"
+
+extern "C" int rs_fail(int code, const char* msg);
+extern "C" void rs_metric_tables(double sensitivity, double mapWeight, uint32_t* ct, uint32_t* mt);
+
+namespace rs {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 8u << 20;   // 8 MiB
+constexpr size_t kNoAllocTableBytes = 2 * kTable * sizeof(uint32_t);
+static __device__ __align__(256) unsigned char g_noAllocScratch[kNoAllocScratchBytes];
+
+// Point k (0 <= k < 8r) of the square ring at Chebyshev distance r >= 1.
+__device__ __forceinline__ void ring_point(int r, int k, int& dx, int& dy) {
+  const int side = k / (2 * r), t = k % (2 * r);
+  if (side == 0) { dx = -r + t; dy = -r; }
+  else if (side == 1) { dx = r; dy = -r + t; }
+  else if (side == 2) { dx = r - t; dy = r; }
+  else { dx = -r; dy = r - t; }
+}
+
+// prepare_neighbors by rings: every offset of the box, ring by ring, goes
+// through the same sorted insertion as build_patch_sparse (key: dx^2 + dy^2,
+// then descending box position -- the sorted offset list's order); the scan
+// stops once the patch is full and a ring lies wholly beyond its last entry.
+__device__ int build_patch_rings(const Problem& pb, int px, int py, Patch& P, unsigned long long* best, int lane) {
+  if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
+  const int lim = pb.patchLimit - 1;
+  const int bw = pb.boxW, bh = pb.boxH;
+  const unsigned W2 = 2u * bw - 1u;
+  const int rmax = max(bw, bh) - 1;
+  int cnt = 0;
+  unsigned long long thr = ~0ull;
+  for (int r = 1; r <= rmax; r++) {
+    if (cnt == lim && (unsigned long long)r * r > (thr >> 32)) break;
+    for (int base = 0; base < 8 * r; base += 32) {
+      const int k = base + lane;
+      unsigned long long key = ~0ull;
+      if (k < 8 * r) {
+        int dx, dy;
+        ring_point(r, k, dx, dy);
+        if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
+          int qx = px + dx, qy = py + dy;
+          if (wrap_or_clip(pb, qx, qy) && pb.has[qy * pb.tw + qx]) {
+            const unsigned idx = (unsigned)(dy + bh - 1) * W2 + (unsigned)(dx + bw - 1);
+            key = ((unsigned long long)(dx * dx + dy * dy) << 32) | (0xFFFFFFFFu - idx);
+          }
+        }
+      }
+      unsigned m = __ballot_sync(kFull, key < thr);
+      while (m) {
+        const int srcLane = __ffs(m) - 1;
+        m &= m - 1;
+        const unsigned long long kk = __shfl_sync(kFull, key, srcLane);
+        if (kk >= thr) continue;
+        const unsigned long long e0 = lane < cnt ? best[lane] : ~0ull;
+        const unsigned long long e1 = lane + 32 < cnt ? best[lane + 32] : ~0ull;
+        const int pos = __popc(__ballot_sync(kFull, e0 < kk)) + __popc(__ballot_sync(kFull, e1 < kk));
+        __syncwarp();
+        if (lane >= pos && lane < cnt && lane + 1 < lim) best[lane + 1] = e0;
+        if (lane + 32 >= pos && lane + 32 < cnt && lane + 33 < lim) best[lane + 33] = e1;
+        __syncwarp();
+        if (lane == 0) best[pos] = kk;
+        __syncwarp();
+        cnt = min(cnt + 1, lim);
+        thr = cnt == lim ? best[lim - 1] : ~0ull;
+      }
+    }
+  }
+  for (int i = lane; i < cnt; i += 32) {
+    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
+    const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
+    int qx = px + dx, qy = py + dy;
+    wrap_or_clip(pb, qx, qy);
+    load_nb(pb, P, 1 + i, pack_off(dx, dy), qy * pb.tw + qx);
+  }
+  __syncwarp();
+  return 1 + cnt;
+}
+
+template <int NC, bool MAP>
+__global__ void __launch_bounds__(256) k_frozen_noalloc(ScoreArgs a) {
+  __shared__ uint32_t ct[kTable], mt[kTable];
+  __shared__ Patch patches[8];
+  __shared__ unsigned long long tops[8][kMaxNeighbors];
+  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
+    ct[i] = a.pb.ctab[i];
+    mt[i] = a.pb.mtab[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  Patch& P = patches[warp];
+  for (int t = blockIdx.x * (blockDim.x >> 5) + warp; t < a.n; t += nw) {
+    const int2 pos = a.targets[t];
+    const int n = build_patch_rings(a.pb, pos.x, pos.y, P, tops[warp], lane);
+    const unsigned c0 = a.candStart[t];
+    const int ncand = (int)(a.candStart[t + 1] - c0);
+    uint32_t bv;
+    int bi;
+    unsigned terms = 0, evals = 0;
+    score_warp<NC, MAP>(a.pb, a.pb.cpx, a.pb.cmap, ct, mt, P, n, ncand,
+                        [&](int k) { return a.cands[c0 + k]; }, lane, bv, bi, terms, evals);
+    if (lane == 0) {
+      a.outSum[t] = bv;
+      a.outPt[t] = bi == INT_MAX ? make_int2(-1, -1) : a.cands[c0 + bi];
+      a.outCount[t] = (unsigned)n;
+    }
+    __syncwarp();
+  }
+}
+
+// The device address of g_noAllocScratch, looked up once per device with that
+// device current (in host code the array's name is only a host-side stand-in).
+unsigned char* noalloc_scratch(int dev, cudaError_t& err) {
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static unsigned char* ptrs[kMaxDevices] = {};
+  err = cudaSuccess;
+  if (dev < 0 || dev >= kMaxDevices) {
+    err = cudaErrorInvalidDevice;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ptrs[dev]) {
+    void* p = nullptr;
+    err = cudaGetSymbolAddress(&p, g_noAllocScratch);
+    if (err != cudaSuccess) return nullptr;
+    ptrs[dev] = static_cast<unsigned char*>(p);
+  }
+  return ptrs[dev];
+}
+
+}  // namespace
+}  // namespace rs
+
+// Frozen-state best fit on caller-owned device buffers; allocates nothing.
+// Declared in include/resynthesizer.h, which states its contract.
+extern "C" __attribute__((visibility("default"))) int resynthFrozenBestFitNoAlloc(
+    const TImageSynthParameters* p, const TFormatIndices* f, const unsigned char* dTarget, unsigned int tw,
+    unsigned int th, const unsigned char* dCorpus, unsigned int cw, unsigned int ch, const unsigned char* dHasValue,
+    const Coordinates* dSourceOf, const Coordinates* dTargets, unsigned int n, const unsigned int* dCandStart,
+    const Coordinates* dCands, unsigned int* dBestSum, Coordinates* dBestPoint, unsigned int* dPatchCount,
+    void* stream) {
+  if (!p || !f || !dTarget || !dCorpus || !dHasValue || !dSourceOf || !dCandStart || !dBestSum || !dBestPoint ||
+      !dPatchCount || (n && (!dTargets || !dCands)))
+    return rs_fail(RESYNTH_ERROR_ARGUMENT, "resynthFrozenBestFitNoAlloc: NULL argument");
+  if (p->patchSize > (unsigned)kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+  if (f->img_match_bpp < 1 || f->img_match_bpp > 3 || f->map_match_bpp > 3 || f->total_bpp > 8 ||
+      f->colorEndBip != 1 + f->img_match_bpp || !tw || !th || !cw || !ch)
+    return rs_fail(RESYNTH_ERROR_UNSUPPORTED, "resynthFrozenBestFitNoAlloc: pixel layout not supported");
+  const bool maps = f->map_match_bpp > 0;
+  const size_t tWords = (size_t)tw * th, cWords = (((size_t)cw * ch) + 3) & ~(size_t)3;
+  const size_t need = kNoAllocTableBytes + 4 * (tWords + cWords) * (maps ? 2 : 1);
+  if (need > kNoAllocScratchBytes)
+    return rs_fail(RESYNTH_ERROR_UNSUPPORTED,
+                   "resynthFrozenBestFitNoAlloc: images too large for the 8 MiB working array "
+                   "(needs 4 KiB + 4 * (target pixels + corpus pixels) * (2 with map channels, else 1) bytes)");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  unsigned char* base = e == cudaSuccess ? noalloc_scratch(dev, e) : nullptr;
+  if (!base) return rs_fail(RESYNTH_ERROR_DEVICE, cudaGetErrorString(e));
+  // Working array layout: tables | target words | [target maps] | corpus words | [corpus maps]
+  uint32_t tables[2 * kTable];
+  rs_metric_tables(p->sensitivityToOutliers, p->mapWeight, tables, tables + kTable);
+  uint32_t* dTables = reinterpret_cast<uint32_t*>(base);
+  uint32_t* tpx = reinterpret_cast<uint32_t*>(base + kNoAllocTableBytes);
+  uint32_t* tmap = maps ? tpx + tWords : nullptr;
+  uint32_t* cpx = tpx + tWords * (maps ? 2 : 1);
+  uint32_t* cmap = maps ? cpx + cWords : nullptr;
+  e = cudaMemcpyAsync(dTables, tables, sizeof tables, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = rs_launch_pack(dTarget, (int)tw, (int)th, f->total_bpp, 1, f->img_match_bpp, f->map_start_bip,
+                       f->map_match_bpp, tpx, tmap, s);
+  if (e == cudaSuccess)
+    e = rs_launch_pack(dCorpus, (int)cw, (int)ch, f->total_bpp, 1, f->img_match_bpp, f->map_start_bip,
+                       f->map_match_bpp, cpx, cmap, s);
+  if (e != cudaSuccess) return rs_fail(RESYNTH_ERROR_DEVICE, cudaGetErrorString(e));
+  if (!n) return 0;
+  ScoreArgs a{};
+  Problem& pb = a.pb;
+  pb.tw = (int)tw;
+  pb.th = (int)th;
+  pb.cw = (int)cw;
+  pb.ch = (int)ch;
+  pb.nc = f->img_match_bpp;
+  pb.nm = f->map_match_bpp;
+  pb.tpx = tpx;
+  pb.tmap = tmap;
+  pb.has = const_cast<uint8_t*>(dHasValue);
+  pb.src = const_cast<int2*>(reinterpret_cast<const int2*>(dSourceOf));
+  pb.cpx = cpx;
+  pb.cmap = cmap;
+  pb.patchLimit = (int)(p->patchSize > 2u ? p->patchSize : 2u);
+  pb.tileH = p->isMakeSeamlesslyTileableHorizontally ? 1 : 0;
+  pb.tileV = p->isMakeSeamlesslyTileableVertically ? 1 : 0;
+  pb.boxW = (int)(tw < cw ? tw : cw);
+  pb.boxH = (int)(th < ch ? th : ch);
+  pb.clipCost = 65535u * f->img_match_bpp + tables[kTable] * f->map_match_bpp;
+  pb.ctab = dTables;
+  pb.mtab = dTables + kTable;
+  a.targets = reinterpret_cast<const int2*>(dTargets);
+  a.n = (int)n;
+  a.candStart = dCandStart;
+  a.cands = reinterpret_cast<const int2*>(dCands);
+  a.outSum = dBestSum;
+  a.outPt = reinterpret_cast<int2*>(dBestPoint);
+  a.outCount = dPatchCount;
+  RS_DISPATCH(pb.nc, maps,
+              (k_frozen_noalloc<NC, MAP><<<grid_for((int)n, 8, sm_count() * 8), 256, 0, s>>>(a)));
+  e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : rs_fail(RESYNTH_ERROR_DEVICE, cudaGetErrorString(e));
+}
