@@ -137,6 +137,79 @@ def cpu_sample(threads: int, side: int = SAMPLE_SIDE):
                 sample=f"{side}x{side} target from the same 128x128 tile (P=16, trys=300), one run")
 
 
+def load_workload(name: str):
+    """(name, target pixmap, corpus pixmap, prepareImageFormatIndices args, params) of a workload."""
+    from resynthesizer_gb300 import workloads as W
+    if name == "render1024":
+        wl = W.render1024()
+        return wl["name"], wl["target"], wl["corpus"], wl["format"], wl["params"]
+    if name == "mapstyle2048":
+        wl = W.mapstyle()
+        return wl["name"], wl["target"], wl["corpus"], wl["format"], wl["params"]
+    if name == "heal256":
+        wl = W.heal256()
+    elif name == "heal4096":
+        wl = W.heal4096()
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
+    return wl["name"], t, c, (3, 0, 0, 0, 0), wl["params"]
+
+
+def psnr(a, b):
+    import numpy as np
+    mse = float(np.mean((a.astype(np.float64) - b.astype(np.float64)) ** 2))
+    return float("inf") if mse == 0 else 10 * np.log10(255.0 ** 2 / mse)
+
+
+def run_quality(args):
+    """Energy of the wavefront result against the CPU engine on the same input:
+    the single-threaded engine once and the 8-thread engine (nondeterministic)
+    `--quality-runs` times.  Energy = sum over target pixels of the full-patch
+    metric at each pixel's final source, patches from the final state."""
+    import numpy as np
+
+    import resynthesizer_gb300 as R
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    name, tgt, cor, spec, kw = load_workload(args.workload)
+    p = R.params(**kw)
+    fmt = R.format_indices(*spec)
+    sel = tgt[..., 0] != 0
+    ys, xs = np.nonzero(sel)
+    targets = np.stack([xs, ys], 1).astype(np.int32)
+    nc = fmt.img_match_bpp
+
+    def energy(out, hv, src):
+        return R.patch_energy(p, fmt, out, cor, hv, src, targets)[0]
+
+    g = R.engine(tgt, cor, fmt, p, opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1))
+    assert g.rc == 0, R.last_error()
+    e_gpu = energy(g.out, g.has_value, g.source)
+    o = O.Oracle()
+    of = o.format_indices(*spec)
+    op = O.make_params(**kw)
+    t0 = time.perf_counter()
+    rc, out_st, st_st, src_st, hv_st = o.engine(op, of, tgt, cor, threads=1, want_state=True)
+    t_st = time.perf_counter() - t0
+    e_st = energy(out_st, hv_st, src_st)
+    e_mt, t_mt, out_mt = [], [], None
+    for _ in range(args.quality_runs):
+        t0 = time.perf_counter()
+        rc, out_mt, st_mt, src_mt, hv_mt = o.engine(op, of, tgt, cor, threads=8, want_state=True)
+        t_mt.append(time.perf_counter() - t0)
+        e_mt.append(energy(out_mt, hv_mt, src_mt))
+    mt_mean = float(np.mean(e_mt))
+    line = {"quality": name, "target_px": int(sel.sum()), "energy_gpu": e_gpu, "energy_cpu_st": e_st,
+            "energy_cpu_mt": e_mt, "energy_cpu_mt_mean": mt_mean, "gpu_over_mt": e_gpu / mt_mean,
+            "gpu_over_st": e_gpu / e_st, "mt_spread": (max(e_mt) - min(e_mt)) / mt_mean,
+            "psnr_gpu_vs_mt": psnr(g.out[sel][:, 1:1 + nc], out_mt[sel][:, 1:1 + nc]),
+            "psnr_st_vs_mt": psnr(out_st[sel][:, 1:1 + nc], out_mt[sel][:, 1:1 + nc]),
+            "gpu_passes": g.stats["passes"], "gpu_ms": g.stats["deviceMs"], "cpu_st_s": t_st,
+            "cpu_mt_s": t_mt, "cpu_kind": "port", "cpu_threads_mt": 8}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -168,13 +241,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--out", type=int, default=1024)
     ap.add_argument("--profile-once", action="store_true",
                     help="one warm-up and one timed engineDevice call only (for ncu captures)")
+    ap.add_argument("--workload", default="render1024",
+                    help="render1024 (default), heal256, heal4096, mapstyle2048")
+    ap.add_argument("--quality", action="store_true", help="energy against the CPU engine instead of speed")
+    ap.add_argument("--quality-runs", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.quality:
+        from resynthesizer_gb300 import build as B
+        B.build()
+        return run_quality(args)
 
     import numpy as np
     import torch
@@ -194,11 +274,13 @@ def main():
         dist.barrier()
     L = R.lib()
 
-    wl = W.render(tile=128, out=args.out)
+    wname, w_target, w_corpus, w_spec, w_params = load_workload(args.workload)
+    wl = {"target": w_target, "corpus": w_corpus, "format": w_spec, "params": w_params}
     p = R.params(**wl["params"])
     fmt = R.format_indices(*wl["format"])
     th, tw, _ = wl["target"].shape
     ch, cw, _ = wl["corpus"].shape
+    target_px = int((wl["target"][..., 0] != 0).sum())
     dev = torch.device("cuda", local)
     t_init = torch.from_numpy(wl["target"]).to(dev)
     t_work = t_init.clone()
@@ -248,7 +330,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
         dist.barrier()
-    value = world * args.steps * tw * th / (total_ms / 1000.0)
+    value = world * args.steps * target_px / (total_ms / 1000.0)
     evals_per_s = world * evals / (total_ms / 1000.0)
 
     # end to end through the reference-facing call with host buffers
@@ -264,7 +346,7 @@ def main():
         if i >= args.warmup:
             e2e_ms.append(dt * 1000)
             h2d, d2h = stt.h2dBytes, stt.d2hBytes
-    e2e_value = world * args.steps * tw * th / (sum(e2e_ms) / 1000.0)
+    e2e_value = world * args.steps * target_px / (sum(e2e_ms) / 1000.0)
 
     # dominant kernel: the per-target synthesis launches, timed live
     flush.fill_(1)
@@ -288,11 +370,12 @@ def main():
         "metric": METRIC, "value": value, "unit": "target px/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "target": f"{tw}x{th}", "corpus": f"{cw}x{ch}", "mode": "wavefront",
+        "config": {"workload": WORKLOAD if wname == "render1024" else wname, "target": f"{tw}x{th}",
+                   "corpus": f"{cw}x{ch}", "target_px": target_px, "mode": "wavefront",
                    "l2": "flushed (256 MB write) between steps, outside the timed intervals",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "evals_per_s": evals_per_s,
-        "energy_per_px": energy / (tw * th),
+        "energy_per_px": energy / target_px,
         "passes": res.stats["passes"],
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": "target px/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -304,7 +387,7 @@ def main():
                      (wave_ms_per_launch / 1000.0)},
         "clocks": clk.summary(),
     }
-    if not args.no_cpu:
+    if not args.no_cpu and wname == "render1024":
         mt = cpu_sample(threads=8)
         stt = cpu_sample(threads=1)
         line["cpu_baseline"] = {"value": mt["value"], "unit": "target px/s", "cores": 8, "kind": mt["kind"],

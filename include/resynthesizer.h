@@ -148,6 +148,7 @@ typedef struct {
   int profile;                /* time each synthesis-kernel launch with CUDA events (stats.waveMs) */
   unsigned int phaseSide;     /* wavefront: k of the k x k colour phases (0 = from the patch radius, 1 = none) */
   unsigned int bandGrowth;    /* wavefront: pass-0 band growth in percent for random orders (0 = 200) */
+  unsigned int minPasses;     /* wavefront: run at least this many passes (0 = the reference's stop rule only) */
 } TResynthOptions;
 
 typedef struct {

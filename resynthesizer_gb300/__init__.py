@@ -58,7 +58,7 @@ class Map(C.Structure):
 class Options(C.Structure):
     _fields_ = [("mode", C.c_int), ("seed", C.c_uint), ("firstBatch", C.c_uint), ("refineBatches", C.c_uint),
                 ("warpsPerBlock", C.c_uint), ("recordState", C.c_int), ("profile", C.c_int),
-                ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint)]
+                ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint)]
 
 
 class Stats(C.Structure):
@@ -150,14 +150,14 @@ def format_indices(colors, mapColors=0, alphaTarget=0, alphaSource=0, isMap=0) -
 
 
 def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, recordState=0,
-            profile=0, phaseSide=0, bandGrowth=0) -> Options:
+            profile=0, phaseSide=0, bandGrowth=0, minPasses=0) -> Options:
     o = Options()
     lib().resynthDefaultOptions(C.byref(o))
     if mode is not None:
         o.mode = mode
     o.seed, o.firstBatch, o.refineBatches, o.warpsPerBlock, o.recordState, o.profile = (
         seed, firstBatch, refineBatches, warpsPerBlock, recordState, profile)
-    o.phaseSide, o.bandGrowth = phaseSide, bandGrowth
+    o.phaseSide, o.bandGrowth, o.minPasses = phaseSide, bandGrowth, minPasses
     return o
 
 

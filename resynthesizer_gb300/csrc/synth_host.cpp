@@ -455,7 +455,15 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
   uint32_t* cmap = pb.nm ? ar.alloc<uint32_t>(cnPad) : nullptr;
   CK(rs_launch_pack(dT, (int)tw, (int)th, f.total_bpp, 1, pb.nc, f.map_start_bip, pb.nm, d.tpx, d.tmap, s));
   CK(rs_launch_pack(dC, (int)cw, (int)ch, f.total_bpp, 1, pb.nc, f.map_start_bip, pb.nm, cpx, cmap, s));
-  launches += 2;
+  // padded copy for the wavefront kernel
+  pb.padW = (int)cw + 2 * rs::kPad;
+  const size_t padWords = (((size_t)pb.padW * (ch + 2 * rs::kPad)) + 3) & ~(size_t)3;
+  uint32_t* cpxPad = ar.alloc<uint32_t>(padWords);
+  uint32_t* cmapPad = pb.nm ? ar.alloc<uint32_t>(padWords) : nullptr;
+  CK(rs_launch_pack_padded(dC, (int)cw, (int)ch, f.total_bpp, pb.nc, f.map_start_bip, pb.nm, cpxPad, cmapPad, s));
+  pb.cpxPad = cpxPad;
+  pb.cmapPad = cmapPad;
+  launches += 3;
   pb.tpx = d.tpx;
   pb.tmap = d.tmap;
   pb.cpx = cpx;
@@ -687,11 +695,11 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     wa.ctr = ctr;
     wa.abortFlag = st.abortDev;
     // Schedule defaults chosen by energy sweeps (random orders: a tiny first
-    // band of 16 pure-probe targets, bands growing 3x; directional orders:
+    // band of 16 pure-probe targets, bands growing 2x; directional orders:
     // bands of at least 1024 in visit order).
     const unsigned first = opt.firstBatch ? opt.firstBatch : (randomOrder ? 16u : 1024u);
     const unsigned refine = opt.refineBatches ? opt.refineBatches : 1u;
-    const double growth = (opt.bandGrowth ? opt.bandGrowth : 300u) / 100.0;
+    const double growth = (opt.bandGrowth ? opt.bandGrowth : 200u) / 100.0;
     const int k = opt.phaseSide ? (int)opt.phaseSide : phase_side(offs, dp.pb.patchLimit);
     constexpr int kMaxBands = 64;
     // While no pixel outside the current pass has a value, a batch's patches
@@ -759,7 +767,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       stats.passLength[pass] = visited;
       stats.betters[pass] = betters;
       if (*cancel || *st.abortHost) break;
-      if ((float)betters / ntargets < 0.1) break;
+      if ((float)betters / ntargets < 0.1 && pass + 1 >= (int)opt.minPasses) break;   // lib/refiner.h:111
     }
     stats.visits = 0;
     for (unsigned i = 0; i < stats.passes; i++) stats.visits += stats.passLength[i];

@@ -10,6 +10,7 @@ namespace rs {
 constexpr int kMaxNeighbors = 64;     // IMAGE_SYNTH_MAX_NEIGHBORS, lib/imageSynthConstants.h:26
 constexpr int kPasses = 6;            // MAX_PASSES, lib/passes.h:51
 constexpr int kTable = 512;           // metric table length, lib/matchWeighting.h:132-133
+constexpr int kPad = 6;               // masked border of the padded corpus copy used by the wavefront kernel
 
 // Device view of one synthesis problem.  Pixels are repacked into 32-bit
 // words: px = mask | c0 << 8 | c1 << 16 | c2 << 24 and map = m0 | m1 << 8 | m2 << 16.
@@ -24,6 +25,9 @@ struct Problem {
   int2* src;                  // sourceOf (tw*th)
   const uint32_t* cpx;        // corpus pixels (cw*ch)
   const uint32_t* cmap;       // corpus map channels (cw*ch) or null
+  const uint32_t* cpxPad;     // the corpus with a kPad-wide masked border ((cw+2kPad) x (ch+2kPad))
+  const uint32_t* cmapPad;    // ... and its map channels, or null
+  int padW;                   // cw + 2 * kPad
   const int2* cpts;           // corpus points (selected and not transparent)
   int ncorpus;
   const int2* offs;           // sorted offsets, offs[0] == (0, 0)
@@ -96,6 +100,8 @@ struct ScoreArgs {
 extern "C" {
 cudaError_t rs_launch_pack(const uint8_t* raw, int w, int h, int bpp, int colorStart, int nc, int mapStart,
                            int nm, uint32_t* px, uint32_t* map, cudaStream_t s);
+cudaError_t rs_launch_pack_padded(const uint8_t* raw, int w, int h, int bpp, int nc, int mapStart, int nm,
+                                  uint32_t* px, uint32_t* map, cudaStream_t s);
 cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc, const uint32_t* px,
                                     cudaStream_t s);
 cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream_t s);

@@ -32,6 +32,14 @@ struct Patch {
   uint32_t px[kMaxNeighbors];    // target pixel word
   uint32_t map[kMaxNeighbors];   // target map word
   int2 src[kMaxNeighbors];       // sourceOf of the neighbour
+  int doff[kMaxNeighbors];       // dy * row stride + dx in the padded corpus (wavefront kernel)
+};
+
+// A corpus copy in memory: pixel (x, y) is word y * stride + x + origin.
+struct CorpusView {
+  const uint32_t* px;
+  const uint32_t* map;
+  int stride, origin;
 };
 
 __device__ __forceinline__ int pack_off(int dx, int dy) { return (int)((unsigned)dy << 16 | ((unsigned)dx & 0xffffu)); }
@@ -168,33 +176,52 @@ __device__ int build_patch_sparse(const Problem& pb, int px, int py, Patch& P, u
 // One neighbour term of computeBestFit for candidate (cx, cy): the clip/mask
 // penalty, or the colour terms (skipped for the target itself) plus the map
 // terms.  Branch-free: an out-of-range point reads word 0 and is discarded.
+// The metric tables are symmetric (they are functions of d * d, and negation
+// is exact), so ct/mt here are their upper halves, indexed by |t - s|: one
+// SIMD absolute difference gives every channel's index at once.
 template <int NC, bool MAP>
-__device__ __forceinline__ uint32_t term_cost(const Problem& pb, const uint32_t* cpx, const uint32_t* cmap,
-                                              const uint32_t* ct, const uint32_t* mt, int cx, int cy, int off,
-                                              uint32_t t, uint32_t tm, bool self) {
-  const int qx = cx + off_dx(off), qy = cy + off_dy(off);
-  const bool inb = (unsigned)qx < (unsigned)pb.cw && (unsigned)qy < (unsigned)pb.ch;
-  const int qi = inb ? qy * pb.cw + qx : 0;
-  const uint32_t s = cpx[qi];
-  uint32_t sum = 0;
-#pragma unroll
-  for (int c = 1; c <= NC; c++) sum += ct[256 + (int)((t >> (8 * c)) & 0xFFu) - (int)((s >> (8 * c)) & 0xFFu)];
+__device__ __forceinline__ uint32_t term_at(const CorpusView& cv, const uint32_t* ct, const uint32_t* mt, int qi,
+                                            bool inb, uint32_t t, uint32_t tm, int nm, uint32_t clip, bool self) {
+  const uint32_t s = cv.px[qi];
+  const uint32_t ad = __vabsdiffu4(t, s);
+  uint32_t sum = ct[(ad >> 8) & 0xFFu];
+  if (NC >= 2) sum += ct[(ad >> 16) & 0xFFu];
+  if (NC >= 3) sum += ct[ad >> 24];
   if (self) sum = 0;
   if (MAP) {
-    const uint32_t sm = cmap[qi];
-    for (int c = 0; c < pb.nm; c++) sum += mt[256 + (int)((tm >> (8 * c)) & 0xFFu) - (int)((sm >> (8 * c)) & 0xFFu)];
+    const uint32_t am = __vabsdiffu4(tm, cv.map[qi]);
+    for (int c = 0; c < nm; c++) sum += mt[(am >> (8 * c)) & 0xFFu];
   }
-  return (inb && (s & 0xFFu) == 0xFFu) ? sum : pb.clipCost;
+  return (inb && (s & 0xFFu) == 0xFFu) ? sum : clip;
 }
+
+template <int NC, bool MAP>
+__device__ __forceinline__ uint32_t term_cost(const Problem& pb, const CorpusView& cv, const uint32_t* ct,
+                                              const uint32_t* mt, int cx, int cy, int off, uint32_t t, uint32_t tm,
+                                              bool self) {
+  const int qx = cx + off_dx(off), qy = cy + off_dy(off);
+  const bool inb = (unsigned)qx < (unsigned)pb.cw && (unsigned)qy < (unsigned)pb.ch;
+  const int qi = inb ? qy * cv.stride + qx + cv.origin : cv.origin;
+  return term_at<NC, MAP>(cv, ct, mt, qi, inb, t, tm, pb.nm, pb.clipCost, self);
+}
+
+// Loads the upper halves (|d| = 0..255) of the metric tables into shared memory.
+__device__ __forceinline__ void load_half_tables(const Problem& pb, uint32_t* ct, uint32_t* mt) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    ct[i] = pb.ctab[256 + i];
+    mt[i] = pb.mtab[256 + i];
+  }
+}
+
+__device__ __forceinline__ CorpusView plain_view(const Problem& pb) { return CorpusView{pb.cpx, pb.cmap, pb.cw, 0}; }
 
 // Full patch metric, one thread, stopping once the sum reaches stopAt.
 template <int NC, bool MAP>
-__device__ uint32_t patch_sum(const Problem& pb, const uint32_t* cpx, const uint32_t* cmap, const uint32_t* ct,
-                              const uint32_t* mt, int cx, int cy, const Patch& P, int n, uint32_t stopAt,
-                              unsigned& terms) {
+__device__ uint32_t patch_sum(const Problem& pb, const CorpusView& cv, const uint32_t* ct, const uint32_t* mt,
+                              int cx, int cy, const Patch& P, int n, uint32_t stopAt, unsigned& terms) {
   uint32_t sum = 0;
   for (int i = 0; i < n; i++) {
-    sum += term_cost<NC, MAP>(pb, cpx, cmap, ct, mt, cx, cy, P.off[i], P.px[i], MAP ? P.map[i] : 0u, i == 0);
+    sum += term_cost<NC, MAP>(pb, cv, ct, mt, cx, cy, P.off[i], P.px[i], MAP ? P.map[i] : 0u, i == 0);
     terms++;
     if (sum >= stopAt) break;
   }
@@ -207,18 +234,28 @@ __device__ uint32_t patch_sum(const Problem& pb, const uint32_t* cpx, const uint
 // the result is the lexicographic minimum of (sum, k), i.e. the first strict
 // minimum in list order, exactly what a sequential computeBestFit loop keeps.
 // bestIdx == INT_MAX when ncand == 0.  Warp-uniform outputs.
-template <int NC, bool MAP, class Get>
-__device__ void score_warp(const Problem& pb, const uint32_t* cpx, const uint32_t* cmap, const uint32_t* ct,
-                           const uint32_t* mt, const Patch& P, int n, int ncand, Get get, int lane,
-                           uint32_t& bestVal, int& bestIdx, unsigned& terms, unsigned& evals) {
+// FAST: every candidate is a corpus point and every patch offset lies within
+// kPad, so with the padded view each term is one load at a precomputed
+// linear offset (the masked border supplies the clip penalty).
+template <int NC, bool MAP, bool FAST, class Get>
+__device__ void score_warp(const Problem& pb, const CorpusView& cv, const uint32_t* ct, const uint32_t* mt,
+                           const Patch& P, int n, int ncand, Get get, int lane, uint32_t& bestVal, int& bestIdx,
+                           unsigned& terms, unsigned& evals) {
   bestVal = 0xFFFFFFFFu;
   bestIdx = INT_MAX;
   int k = lane;
   int2 c = make_int2(0, 0);
+  int cb = 0;
   if (k < ncand) {
     c = get(k);
+    cb = c.y * cv.stride + c.x + cv.origin;
     evals++;
   }
+  auto term = [&](int ii) -> uint32_t {
+    if (FAST) return term_at<NC, MAP>(cv, ct, mt, cb + P.doff[ii], true, P.px[ii], MAP ? P.map[ii] : 0u, pb.nm,
+                                      pb.clipCost, ii == 0);
+    return term_cost<NC, MAP>(pb, cv, ct, mt, c.x, c.y, P.off[ii], P.px[ii], MAP ? P.map[ii] : 0u, ii == 0);
+  };
   uint32_t sum = 0;
   int i = 0;
   int next = 32;
@@ -226,12 +263,15 @@ __device__ void score_warp(const Problem& pb, const uint32_t* cpx, const uint32_
     const bool active = k < ncand;
     if (active) {
       uint32_t add = 0;
+      if (i + 4 <= n) {
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int ii = min(i + u, n - 1);
-        const uint32_t v = term_cost<NC, MAP>(pb, cpx, cmap, ct, mt, c.x, c.y, P.off[ii], P.px[ii],
-                                              MAP ? P.map[ii] : 0u, ii == 0);
-        add += (i + u < n) ? v : 0u;
+        for (int u = 0; u < 4; u++) add += term(i + u);
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const uint32_t v = term(min(i + u, n - 1));
+          add += (i + u < n) ? v : 0u;
+        }
       }
       const int step = min(4, n - i);
       sum += add;
@@ -263,6 +303,7 @@ __device__ void score_warp(const Problem& pb, const uint32_t* cpx, const uint32_
       i = 0;
       if (k < ncand) {
         c = get(k);
+        cb = c.y * cv.stride + c.x + cv.origin;
         evals++;
       }
     }
@@ -279,22 +320,23 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
   return x;
 }
 
-// Counter-based probe draw (seed, pass, target pixel, probe) -> a uniform
-// corpus point: straight from the corpus rectangle when every pixel is a
-// corpus point, else through the corpus point list.
-__device__ __forceinline__ int2 probe_point(const Problem& pb, uint32_t seed, uint32_t pass, uint32_t pix,
-                                            uint32_t j) {
-  const uint32_t h = mix32(seed ^ mix32(pass * 0x9E3779B9u + 0x7f4a7c15u) ^ mix32(pix * 0x85EBCA77u + j * 0xC2B2AE3Du));
-  if (pb.fullCorpus) {
-    const uint32_t h2 = mix32(h + 0x632BE5ABu);
-    return make_int2((int)__umulhi(h, (uint32_t)pb.cw), (int)__umulhi(h2, (uint32_t)pb.ch));
-  }
+// Counter-based probe draws: a base key per (seed, pass, target pixel), one
+// hash per probe.  A uniform corpus point comes straight from the corpus
+// rectangle when every pixel is a corpus point (x from the hash's high half,
+// y from its low half rotated up), else through the corpus point list.
+__device__ __forceinline__ uint32_t probe_base(uint32_t seed, uint32_t pass, uint32_t pix) {
+  return mix32(seed ^ mix32(pass * 0x9E3779B9u + 0x7f4a7c15u) ^ (pix * 0x85EBCA77u));
+}
+__device__ __forceinline__ int2 probe_point(const Problem& pb, uint32_t base, uint32_t j) {
+  const uint32_t h = mix32(base + j * 0x9E3779B9u);
+  if (pb.fullCorpus)
+    return make_int2((int)__umulhi(h, (uint32_t)pb.cw), (int)__umulhi(__funnelshift_l(h, h, 16), (uint32_t)pb.ch));
   return __ldg(&pb.cpts[__umulhi(h, (uint32_t)pb.ncorpus)]);
 }
 
-__device__ __forceinline__ bool corpus_ok(const Problem& pb, const uint32_t* cpx, int2 c) {
+__device__ __forceinline__ bool corpus_ok(const Problem& pb, const CorpusView& cv, int2 c) {
   return (unsigned)c.x < (unsigned)pb.cw && (unsigned)c.y < (unsigned)pb.ch &&
-         (cpx[c.y * pb.cw + c.x] & 0xFFu) == 0xFFu;
+         (cv.px[c.y * cv.stride + c.x + cv.origin] & 0xFFu) == 0xFFu;
 }
 
 // ----------------------------------------------------------- shared memory
@@ -359,10 +401,7 @@ template <int NC, bool MAP>
 __global__ void __launch_bounds__(256) k_frozen(ScoreArgs a) {
   __shared__ uint32_t ct[kTable], mt[kTable];
   __shared__ Patch patches[8];
-  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
-    ct[i] = a.pb.ctab[i];
-    mt[i] = a.pb.mtab[i];
-  }
+  load_half_tables(a.pb, ct, mt);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = gridDim.x * (blockDim.x >> 5);
@@ -375,8 +414,8 @@ __global__ void __launch_bounds__(256) k_frozen(ScoreArgs a) {
     uint32_t bv;
     int bi;
     unsigned terms = 0, evals = 0;
-    score_warp<NC, MAP>(a.pb, a.pb.cpx, a.pb.cmap, ct, mt, P, n, ncand,
-                        [&](int k) { return a.cands[c0 + k]; }, lane, bv, bi, terms, evals);
+    score_warp<NC, MAP, false>(a.pb, plain_view(a.pb), ct, mt, P, n, ncand,
+                               [&](int k) { return a.cands[c0 + k]; }, lane, bv, bi, terms, evals);
     if (lane == 0) {
       a.outSum[t] = bv;
       a.outPt[t] = bi == INT_MAX ? make_int2(-1, -1) : a.cands[c0 + bi];
@@ -392,10 +431,7 @@ template <int NC, bool MAP>
 __global__ void __launch_bounds__(256) k_energy(ScoreArgs a) {
   __shared__ uint32_t ct[kTable], mt[kTable];
   __shared__ Patch patches[8];
-  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
-    ct[i] = a.pb.ctab[i];
-    mt[i] = a.pb.mtab[i];
-  }
+  load_half_tables(a.pb, ct, mt);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = gridDim.x * (blockDim.x >> 5);
@@ -407,7 +443,7 @@ __global__ void __launch_bounds__(256) k_energy(ScoreArgs a) {
     const int2 s = a.pb.src[pos.y * a.pb.tw + pos.x];
     unsigned long long v = 0;
     for (int i = lane; i < n; i += 32)
-      v += term_cost<NC, MAP>(a.pb, a.pb.cpx, a.pb.cmap, ct, mt, s.x, s.y, P.off[i], P.px[i], MAP ? P.map[i] : 0u,
+      v += term_cost<NC, MAP>(a.pb, plain_view(a.pb), ct, mt, s.x, s.y, P.off[i], P.px[i], MAP ? P.map[i] : 0u,
                               i == 0);
     v = warp_sum_u64(v);
     if (lane == 0) {
@@ -450,10 +486,7 @@ __global__ void __launch_bounds__(256, 1) k_replay(ReplayArgs a, int t0, int t1)
   __shared__ unsigned s_cursor;
   const Problem& pb = a.pb;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < kTable; i += blockDim.x) {
-    ct[i] = pb.ctab[i];
-    mt[i] = pb.mtab[i];
-  }
+  load_half_tables(pb, ct, mt);
   if (tid == 0) s_cursor = a.ctr->cursor;
   __syncthreads();
   unsigned cursor = s_cursor;
@@ -504,7 +537,7 @@ __global__ void __launch_bounds__(256, 1) k_replay(ReplayArgs a, int t0, int t1)
         int2 c = make_int2(0, 0);
         if (k < count && P.src[k].x != -1) {
           c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
-          valid = corpus_ok(pb, pb.cpx, c) && a.recentProber[c.y * pb.cw + c.x] != (unsigned)t;
+          valid = corpus_ok(pb, plain_view(pb), c) && a.recentProber[c.y * pb.cw + c.x] != (unsigned)t;
         }
         const unsigned long long key =
             valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
@@ -524,7 +557,7 @@ __global__ void __launch_bounds__(256, 1) k_replay(ReplayArgs a, int t0, int t1)
     // 3. score heuristic-1 candidates (full sums) -> first strict minimum.
     unsigned long long key = ~0ull;
     if (tid < nh) {
-      const uint32_t s = patch_sum<NC, MAP>(pb, pb.cpx, pb.cmap, ct, mt, hl[tid].x, hl[tid].y, P, count,
+      const uint32_t s = patch_sum<NC, MAP>(pb, plain_view(pb), ct, mt, hl[tid].x, hl[tid].y, P, count,
                                             0xFFFFFFFFu, terms);
       key = ((unsigned long long)s << 32) | (unsigned)tid;
     }
@@ -551,7 +584,7 @@ __global__ void __launch_bounds__(256, 1) k_replay(ReplayArgs a, int t0, int t1)
           if (pos_ >= a.randCount) atomicOr(&a.ctr->error, 2u);
           const int2 c = pb.cpts[(unsigned)r / div];
           rpt[tid] = c;
-          const uint32_t s = patch_sum<NC, MAP>(pb, pb.cpx, pb.cmap, ct, mt, c.x, c.y, P, count, bestVal, terms);
+          const uint32_t s = patch_sum<NC, MAP>(pb, plain_view(pb), ct, mt, c.x, c.y, P, count, bestVal, terms);
           evals++;
           if (s < bestVal) rk = ((unsigned long long)s << 32) | j;
         }
@@ -599,9 +632,12 @@ __global__ void __launch_bounds__(256, 1) k_replay(ReplayArgs a, int t0, int t1)
 
 // --------------------------------------------------------------- wavefront
 
+// Per-warp shared memory of k_wave: the patch, then one 512-byte area that
+// holds the sparse top list while the patch is built and the continuation
+// candidates afterwards.
 struct WaveSmem {
-  static constexpr int kPerWarp =
-      (int)sizeof(Patch) + kMaxNeighbors * (int)sizeof(int2) + kMaxNeighbors * (int)sizeof(unsigned long long);
+  static constexpr int kPerWarp = (int)sizeof(Patch) + kMaxNeighbors * (int)sizeof(unsigned long long);
+  static constexpr int kHead = 2 * 256 * 4 + 16;   // half tables + two mbarriers
 };
 
 // One wavefront batch: a warp per target.  Candidates are the deduplicated
@@ -609,20 +645,29 @@ struct WaveSmem {
 // counter-based random probes; the best (first strict minimum) different
 // source is staged for k_commit.
 template <int NC, bool MAP, bool SMEMC>
-__global__ void __launch_bounds__(512, 1) k_wave(WaveArgs a) {
+__global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b0 = a.batchStart[a.batch], b1 = a.batchStart[a.batch + 1];
   const int nslots = b1 - b0;
+  // Team size: when the batch has fewer targets than the grid has warps, G
+  // warps (a power of two, at most the CTA) share one target's candidates.
+  // The result does not depend on G: every team reduces to the same
+  // (sum, candidate index) minimum.
+  const int wpb = blockDim.x >> 5;
+  int G = 1;
+  while (G < wpb && (long long)nslots * (G * 2) <= (long long)gridDim.x * wpb) G *= 2;
+  const int teamsPerBlock = wpb / G;
   // CTAs beyond this batch's size leave before staging anything.
-  if ((int)(blockIdx.x * (blockDim.x >> 5)) >= nslots) return;
+  if ((int)(blockIdx.x * teamsPerBlock) >= nslots) return;
   uint32_t* ct = reinterpret_cast<uint32_t*>(smem);
-  uint32_t* mt = ct + kTable;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(mt + kTable);
-  unsigned char* p = smem + 2 * kTable * 4 + 16;
+  uint32_t* mt = ct + 256;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(mt + 256);
+  unsigned char* p = smem + WaveSmem::kHead;
   const Problem& pb = a.pb;
-  const uint32_t* cpx = pb.cpx;
-  const uint32_t* cmap = pb.cmap;
-  const unsigned cwords = ((unsigned)(pb.cw * pb.ch) + 3u) & ~3u;
+  // The padded corpus: staged into shared memory when it fits.
+  const int padH = pb.ch + 2 * kPad;
+  CorpusView cv{pb.cpxPad, pb.cmapPad, pb.padW, kPad * pb.padW + kPad};
+  const unsigned cwords = ((unsigned)(pb.padW * padH) + 3u) & ~3u;
   if (SMEMC) {
     uint32_t* scpx = reinterpret_cast<uint32_t*>(p);
     p += cwords * 4;
@@ -631,76 +676,110 @@ __global__ void __launch_bounds__(512, 1) k_wave(WaveArgs a) {
       scmap = reinterpret_cast<uint32_t*>(p);
       p += cwords * 4;
     }
-    bool ok = stage_words(scpx, pb.cpx, cwords, bar);
-    if (MAP && ok) ok = stage_words(scmap, pb.cmap, cwords, bar + 1);
+    bool ok = stage_words(scpx, pb.cpxPad, cwords, bar);
+    if (MAP && ok) ok = stage_words(scmap, pb.cmapPad, cwords, bar + 1);
     if (!ok) {
       if (threadIdx.x == 0) atomicOr(&a.ctr->error, 1u);
       return;
     }
-    cpx = scpx;
-    cmap = scmap;
+    cv.px = scpx;
+    cv.map = scmap;
   }
   __shared__ int s_abort;
-  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
-    ct[i] = pb.ctab[i];
-    mt[i] = pb.mtab[i];
-  }
+  load_half_tables(pb, ct, mt);
   // One read of the host-mapped flag per CTA, so the whole CTA agrees.
   if (threadIdx.x == 0) s_abort = *a.abortFlag;
   __syncthreads();
   if (s_abort) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char* wbase = p + warp * WaveSmem::kPerWarp;
+  const int team = warp / G, tw = warp % G, lead = team * G;
+  // The team's patch and candidate list live in its first warp's region.
+  unsigned char* wbase = p + lead * WaveSmem::kPerWarp;
   Patch& P = *reinterpret_cast<Patch*>(wbase);
-  int2* prop = reinterpret_cast<int2*>(wbase + sizeof(Patch));
-  unsigned long long* topk = reinterpret_cast<unsigned long long*>(wbase + sizeof(Patch) + kMaxNeighbors * sizeof(int2));
+  unsigned long long* topk = reinterpret_cast<unsigned long long*>(wbase + sizeof(Patch));
+  int2* prop = reinterpret_cast<int2*>(topk);
+  __shared__ unsigned long long s_key[16];
+  __shared__ int s_n[16], s_np[16], s_fast[16];
+  auto team_sync = [&]() {
+    if (G == 1) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(G * 32) : "memory");
+  };
   const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
-  const int nw = gridDim.x * (blockDim.x >> 5);
   unsigned terms = 0, evals = 0;
-  for (int slot = blockIdx.x * (blockDim.x >> 5) + warp; slot < nslots; slot += nw) {
+  for (int slot = blockIdx.x * teamsPerBlock + team; slot < nslots; slot += gridDim.x * teamsPerBlock) {
     const int t = b0 + slot;
     const int2 pos = a.targets[t];
     const int pi = pos.y * pb.tw + pos.x;
-    const int n = sparse ? build_patch_sparse(pb, pos.x, pos.y, P, topk, a.targets, b0, lane)
-                         : build_patch_warp(pb, pos.x, pos.y, P, lane);
-    // continuation candidates, deduplicated, in neighbour order
-    int np = 0;
-    for (int r = 0; r < n; r += 32) {
-      const int k = r + lane;
-      bool valid = false;
-      int2 c = make_int2(0, 0);
-      if (k < n && P.src[k].x >= 0) {
-        c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
-        valid = corpus_ok(pb, cpx, c);
+    if (tw == 0) {
+      const int n = sparse ? build_patch_sparse(pb, pos.x, pos.y, P, topk, a.targets, b0, lane)
+                           : build_patch_warp(pb, pos.x, pos.y, P, lane);
+      // linear offsets into the padded corpus; the fast path needs all within kPad
+      int far = 0;
+      for (int i = lane; i < n; i += 32) {
+        const int dx = off_dx(P.off[i]), dy = off_dy(P.off[i]);
+        P.doff[i] = dy * pb.padW + dx;
+        far |= (abs(dx) > kPad) | (abs(dy) > kPad);
       }
-      const unsigned long long key =
-          valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
-      const unsigned peers = __match_any_sync(kFull, key);
-      bool keep = valid && (peers & lanemask_lt()) == 0u;
-      for (int e = 0; e < np && keep; e++)
-        if (prop[e].x == c.x && prop[e].y == c.y) keep = false;
-      const unsigned km = __ballot_sync(kFull, keep);
-      if (keep) prop[np + __popc(km & lanemask_lt())] = c;
-      np += __popc(km);
-      __syncwarp();
+      far = __any_sync(kFull, far);
+      // continuation candidates, deduplicated, in neighbour order
+      int np = 0;
+      for (int r = 0; r < n; r += 32) {
+        const int k = r + lane;
+        bool valid = false;
+        int2 c = make_int2(0, 0);
+        if (k < n && P.src[k].x >= 0) {
+          c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
+          valid = corpus_ok(pb, cv, c);
+        }
+        const unsigned long long key =
+            valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
+        const unsigned peers = __match_any_sync(kFull, key);
+        bool keep = valid && (peers & lanemask_lt()) == 0u;
+        for (int e = 0; e < np && keep; e++)
+          if (prop[e].x == c.x && prop[e].y == c.y) keep = false;
+        const unsigned km = __ballot_sync(kFull, keep);
+        if (keep) prop[np + __popc(km & lanemask_lt())] = c;
+        np += __popc(km);
+        __syncwarp();
+      }
+      if (lane == 0) {
+        s_n[lead] = n;
+        s_np[lead] = np;
+        s_fast[lead] = !far;
+      }
     }
+    team_sync();
+    const int n = s_n[lead], np = s_np[lead];
+    const bool fast = s_fast[lead] != 0;
     const int ncand = np + (int)a.trys;
+    const uint32_t pbase = probe_base(a.seed, a.pass, (uint32_t)pi);
+    // Warp tw of the team scores candidates tw, tw + G, tw + 2G, ...
+    const int nloc = ncand > tw ? (ncand - tw + G - 1) / G : 0;
     uint32_t bv;
     int bi;
-    score_warp<NC, MAP>(
-        pb, cpx, cmap, ct, mt, P, n, ncand,
-        [&](int k) { return k < np ? prop[k] : probe_point(pb, a.seed, a.pass, (uint32_t)pi, (uint32_t)(k - np)); },
-        lane, bv, bi, terms, evals);
-    if (lane == 0) {
+    auto get = [&](int j) {
+      const int k = tw + j * G;
+      return k < np ? prop[k] : probe_point(pb, pbase, (uint32_t)(k - np));
+    };
+    if (fast)
+      score_warp<NC, MAP, true>(pb, cv, ct, mt, P, n, nloc, get, lane, bv, bi, terms, evals);
+    else
+      score_warp<NC, MAP, false>(pb, cv, ct, mt, P, n, nloc, get, lane, bv, bi, terms, evals);
+    if (lane == 0) s_key[warp] = bi == INT_MAX ? ~0ull : ((unsigned long long)bv << 32) | (unsigned)(tw + bi * G);
+    team_sync();
+    if (tw == 0 && lane == 0) {
+      unsigned long long best = ~0ull;
+      for (int w = 0; w < G; w++) best = min(best, s_key[lead + w]);
       int2 out = make_int2(-2, -2);
-      if (bi != INT_MAX) {
-        const int2 best = bi < np ? prop[bi] : probe_point(pb, a.seed, a.pass, (uint32_t)pi, (uint32_t)(bi - np));
+      if (best != ~0ull) {
+        const int k = (int)(best & 0xffffffffu);
+        const int2 pt = k < np ? prop[k] : probe_point(pb, pbase, (uint32_t)(k - np));
         const int2 cur = pb.src[pi];
-        if (cur.x != best.x || cur.y != best.y) out = best;
+        if (cur.x != pt.x || cur.y != pt.y) out = pt;
       }
       a.stageSrc[slot] = out;
     }
-    __syncwarp();
+    team_sync();
   }
   unsigned long long tv = warp_sum_u64(terms), ev = warp_sum_u64(evals);
   if (lane == 0) {
@@ -748,6 +827,24 @@ __global__ void k_pack(const uint8_t* raw, int npx, int bpp, int colorStart, int
       for (int c = 0; c < nm; c++) m |= (uint32_t)q[mapStart + c] << (8 * c);
       map[i] = m;
     }
+  }
+}
+
+// The corpus with a kPad-wide border of zero (masked) words.
+__global__ void k_pack_padded(const uint8_t* raw, int w, int h, int bpp, int nc, int mapStart, int nm,
+                              uint32_t* px, uint32_t* map) {
+  const int pw = w + 2 * kPad, ph = h + 2 * kPad;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < pw * ph; i += gridDim.x * blockDim.x) {
+    const int x = i % pw - kPad, y = i / pw - kPad;
+    uint32_t word = 0, m = 0;
+    if (x >= 0 && x < w && y >= 0 && y < h) {
+      const uint8_t* q = raw + ((size_t)y * w + x) * bpp;
+      word = q[0];
+      for (int c = 0; c < nc; c++) word |= (uint32_t)q[1 + c] << (8 * (c + 1));
+      for (int c = 0; c < nm; c++) m |= (uint32_t)q[mapStart + c] << (8 * c);
+    }
+    px[i] = word;
+    if (map) map[i] = m;
   }
 }
 
@@ -801,6 +898,13 @@ extern "C" cudaError_t rs_launch_pack(const uint8_t* raw, int w, int h, int bpp,
   return cudaGetLastError();
 }
 
+extern "C" cudaError_t rs_launch_pack_padded(const uint8_t* raw, int w, int h, int bpp, int nc, int mapStart,
+                                             int nm, uint32_t* px, uint32_t* map, cudaStream_t s) {
+  const int n = (w + 2 * kPad) * (h + 2 * kPad);
+  k_pack_padded<<<grid_for(n, 256, sm_count() * 8), 256, 0, s>>>(raw, w, h, bpp, nc, mapStart, nm, px, map);
+  return cudaGetLastError();
+}
+
 extern "C" cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc, const uint32_t* px,
                                                cudaStream_t s) {
   const int n = w * h;
@@ -825,9 +929,9 @@ extern "C" cudaError_t rs_launch_energy(const ScoreArgs& a, cudaStream_t s) {
 
 namespace {
 size_t wave_smem(const Problem& pb, bool smemc, int warps) {
-  size_t b = 2 * kTable * 4 + 16;
+  size_t b = WaveSmem::kHead;
   if (smemc) {
-    const size_t cwords = ((size_t)pb.cw * pb.ch + 3) & ~(size_t)3;
+    const size_t cwords = ((size_t)pb.padW * (pb.ch + 2 * kPad) + 3) & ~(size_t)3;
     b += cwords * 4 * (pb.nm > 0 ? 2 : 1);
   }
   return b + (size_t)warps * WaveSmem::kPerWarp;
@@ -859,7 +963,7 @@ extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, cudaStream_t
   if (warps < 1) warps = 16;
   if (warps > 16) warps = 16;
   const size_t smemCorpus = wave_smem(a.pb, true, warps);
-  const bool smemc = smemCorpus <= 110 * 1024;
+  const bool smemc = smemCorpus <= 112 * 1024;   // two CTAs per SM
   const size_t smem = smemc ? smemCorpus : wave_smem(a.pb, false, warps);
   cudaError_t e = cudaSuccess;
   if (smemc) {
@@ -976,10 +1080,7 @@ __global__ void __launch_bounds__(256) k_frozen_noalloc(ScoreArgs a) {
   __shared__ uint32_t ct[kTable], mt[kTable];
   __shared__ Patch patches[8];
   __shared__ unsigned long long tops[8][kMaxNeighbors];
-  for (int i = threadIdx.x; i < kTable; i += blockDim.x) {
-    ct[i] = a.pb.ctab[i];
-    mt[i] = a.pb.mtab[i];
-  }
+  load_half_tables(a.pb, ct, mt);
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = gridDim.x * (blockDim.x >> 5);
@@ -992,8 +1093,8 @@ __global__ void __launch_bounds__(256) k_frozen_noalloc(ScoreArgs a) {
     uint32_t bv;
     int bi;
     unsigned terms = 0, evals = 0;
-    score_warp<NC, MAP>(a.pb, a.pb.cpx, a.pb.cmap, ct, mt, P, n, ncand,
-                        [&](int k) { return a.cands[c0 + k]; }, lane, bv, bi, terms, evals);
+    score_warp<NC, MAP, false>(a.pb, plain_view(a.pb), ct, mt, P, n, ncand,
+                               [&](int k) { return a.cands[c0 + k]; }, lane, bv, bi, terms, evals);
     if (lane == 0) {
       a.outSum[t] = bv;
       a.outPt[t] = bi == INT_MAX ? make_int2(-1, -1) : a.cands[c0 + bi];

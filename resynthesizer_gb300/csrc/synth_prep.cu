@@ -148,27 +148,50 @@ __global__ void k_compact(PixPred pred, int npx, int w, const int* blockOffsets,
 // Batch keys of one pass.  rank = position in the visit order: given (the
 // host order) or drawn from a hash of the pixel (random orders).  Targets of
 // rank >= endRank are not visited this pass.  key = band * K + phase.
+// Warp-aggregated atomicAdd of 1 on counter[key] (key < 0: no-op): one
+// atomic per distinct key in the warp; returns the old value plus this
+// lane's rank among the lanes sharing its key.
+__device__ __forceinline__ int warp_bump(int* counter, int key) {
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (lane == leader && key >= 0) base = atomicAdd(&counter[key], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  return base + __popc(peers & lt);
+}
+
 __global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
                              const int* bandEnds, int nbands, int k, int* keys, int* hist) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const int2 p = targets[t];
-    const int rank = randomOrder ? (int)__umulhi(mix32p((uint32_t)(p.y * tw + p.x) * 0x9E3779B1u ^ seed), (uint32_t)n)
-                                 : t;
+  const int stride = gridDim.x * blockDim.x;
+  const int limit = (n + stride - 1) / stride * stride;   // whole warps iterate together
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < limit; t += stride) {
     int key = -1;
-    if (rank < endRank) {
-      int band = 0;
-      while (band < nbands - 1 && rank >= bandEnds[band]) band++;
-      key = band * k * k + (p.y % k) * k + (p.x % k);
-      atomicAdd(&hist[key], 1);
+    if (t < n) {
+      const int2 p = targets[t];
+      const int rank = randomOrder ? (int)__umulhi(mix32p((uint32_t)(p.y * tw + p.x) * 0x9E3779B1u ^ seed),
+                                                   (uint32_t)n)
+                                   : t;
+      if (rank < endRank) {
+        int band = 0;
+        while (band < nbands - 1 && rank >= bandEnds[band]) band++;
+        key = band * k * k + (p.y % k) * k + (p.x % k);
+      }
+      keys[t] = key;
     }
-    keys[t] = key;
+    warp_bump(hist, key);
   }
 }
 
 __global__ void k_scatter(const int2* targets, int n, const int* keys, int* cursor, int2* out) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    const int key = keys[t];
-    if (key >= 0) out[atomicAdd(&cursor[key], 1)] = targets[t];
+  const int stride = gridDim.x * blockDim.x;
+  const int limit = (n + stride - 1) / stride * stride;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < limit; t += stride) {
+    const int key = t < n ? keys[t] : -1;
+    const int pos = warp_bump(cursor, key);
+    if (key >= 0) out[pos] = targets[t];
   }
 }
 
