@@ -199,14 +199,22 @@ def run_quality(args):
         rc, out_mt, st_mt, src_mt, hv_mt = o.engine(op, of, tgt, cor, threads=8, want_state=True)
         t_mt.append(time.perf_counter() - t0)
         e_mt.append(energy(out_mt, hv_mt, src_mt))
-    mt_mean = float(np.mean(e_mt))
+    mt_mean = float(np.mean(e_mt)) if e_mt else None
+    ref_out = out_mt if out_mt is not None else out_st
     line = {"quality": name, "target_px": int(sel.sum()), "energy_gpu": e_gpu, "energy_cpu_st": e_st,
-            "energy_cpu_mt": e_mt, "energy_cpu_mt_mean": mt_mean, "gpu_over_mt": e_gpu / mt_mean,
-            "gpu_over_st": e_gpu / e_st, "mt_spread": (max(e_mt) - min(e_mt)) / mt_mean,
-            "psnr_gpu_vs_mt": psnr(g.out[sel][:, 1:1 + nc], out_mt[sel][:, 1:1 + nc]),
-            "psnr_st_vs_mt": psnr(out_st[sel][:, 1:1 + nc], out_mt[sel][:, 1:1 + nc]),
-            "gpu_passes": g.stats["passes"], "gpu_ms": g.stats["deviceMs"], "cpu_st_s": t_st,
-            "cpu_mt_s": t_mt, "cpu_kind": "port", "cpu_threads_mt": 8}
+            "energy_cpu_mt": e_mt, "energy_cpu_mt_mean": mt_mean,
+            "gpu_over_mt": e_gpu / mt_mean if mt_mean else None, "gpu_over_st": e_gpu / e_st,
+            "mt_spread": (max(e_mt) - min(e_mt)) / mt_mean if mt_mean else None,
+            "psnr_gpu_vs_ref": psnr(g.out[sel][:, 1:1 + nc], ref_out[sel][:, 1:1 + nc]),
+            "psnr_ref": "8-thread CPU run" if out_mt is not None else "single-threaded CPU run",
+            "gpu_passes": g.stats["passes"], "gpu_ms": g.stats["deviceMs"], "gpu_evals": g.stats["evals"],
+            "cpu_st_s": t_st, "cpu_st_evals": st_st.evals, "cpu_mt_s": t_mt, "cpu_kind": "port",
+            "cpu_threads_mt": 8}
+    if int(sel.sum()) <= 100000:
+        # sequential replay: byte-identical to the single-threaded engine
+        r = R.engine(tgt, cor, fmt, p, opts=R.options(mode=R.MODE_REPLAY))
+        line["replay_identical_to_cpu_st"] = bool(r.rc == 0 and np.array_equal(r.out, out_st))
+        line["replay_ms"] = r.stats["deviceMs"]
     print(json.dumps(line), flush=True)
 
 
