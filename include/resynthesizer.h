@@ -254,6 +254,26 @@ int resynthFrozenBestFitNoAlloc(const TImageSynthParameters *parameters, const T
                                 unsigned int *dBestSum, Coordinates *dBestPoint, unsigned int *dPatchCount,
                                 void *stream);
 
+/* One request of imageSynthBatch: the arguments of imageSynth2 (mask2 NULL =
+ * imageSynth) and the request's own return code. */
+typedef struct {
+  ImageBuffer *image;
+  ImageBuffer *mask;
+  ImageBuffer *mask2;
+  TImageFormat format;
+  TImageSynthParameters *parameters;   /* NULL = defaults */
+  int result;                          /* out: the request's return code */
+} TResynthRequest;
+
+/* No counterpart in the reference (which heals one image per call).  Runs
+ * `count` independent requests concurrently on `concurrency` host workers
+ * (0 = 8), each with its own CUDA stream, so the small batches of many
+ * requests overlap on the GPU.  Each request's result equals an imageSynthEx
+ * call with the same options.  stats (may be NULL) sums all requests.
+ * Returns 0, or the first nonzero request result. */
+int imageSynthBatch(TResynthRequest *requests, unsigned int count, unsigned int concurrency,
+                    const TResynthOptions *options, TResynthStats *stats);
+
 /* Text of the last error on this thread ("" if none). */
 const char *resynthLastError(void);
 

@@ -61,6 +61,11 @@ class Options(C.Structure):
                 ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint)]
 
 
+class Request(C.Structure):
+    _fields_ = [("image", C.POINTER(ImageBuffer)), ("mask", C.POINTER(ImageBuffer)), ("mask2", C.POINTER(ImageBuffer)),
+                ("format", C.c_int), ("parameters", C.POINTER(ImageSynthParameters)), ("result", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("visits", C.c_ulonglong), ("evals", C.c_ulonglong), ("terms", C.c_ulonglong),
                 ("passes", C.c_uint), ("passLength", C.c_uint * 6), ("betters", C.c_uint * 6),
@@ -101,6 +106,7 @@ def lib() -> C.CDLL:
         L.engine.argtypes = [ImageSynthParameters, P(FormatIndices), P(Map), P(Map), vp, vp, P(C.c_int)]
         L.engineEx.argtypes = [P(ImageSynthParameters), P(FormatIndices), P(Map), P(Map), vp, vp, P(C.c_int),
                                P(Options), P(Stats)]
+        L.imageSynthBatch.argtypes = [C.POINTER(Request), u, u, P(Options), P(Stats)]
         L.engineDevice.argtypes = [P(ImageSynthParameters), P(FormatIndices), vp, u, u, vp, u, u, vp, vp, vp,
                                    P(C.c_int), P(Options), P(Stats)]
         L.resynthFrozenBestFit.argtypes = [P(ImageSynthParameters), P(FormatIndices), vp, u, u, vp, u, u, vp, vp, vp,
@@ -299,3 +305,23 @@ def patch_energy(p, fmt, target, corpus, has_value, source, targets):
     if rc:
         raise RuntimeError(f"resynthPatchEnergy rc={rc}: {last_error()}")
     return int(e.value), per
+
+
+def image_synth_batch(items, opts: Options | None = None, concurrency: int = 8):
+    """imageSynthBatch over [(image, mask, fmt, params or None), ...]; returns
+    (rc, outputs, per-request codes, stats)."""
+    keep, reqs = [], (Request * len(items))()
+    for i, (image, mask, fmt, p) in enumerate(items):
+        img = np.ascontiguousarray(image, np.uint8).copy()
+        m = np.ascontiguousarray(mask, np.uint8)
+        ib, mb = _buf(img), _buf(m)
+        pp = C.pointer(p) if p is not None else None
+        keep.append((img, m, ib, mb, pp))
+        reqs[i].image = C.pointer(ib)
+        reqs[i].mask = C.pointer(mb)
+        reqs[i].mask2 = None
+        reqs[i].format = fmt
+        reqs[i].parameters = pp
+    st = Stats()
+    rc = lib().imageSynthBatch(reqs, len(items), concurrency, C.byref(opts) if opts else None, C.byref(st))
+    return rc, [k[0] for k in keep], [reqs[i].result for i in range(len(items))], st.as_dict()

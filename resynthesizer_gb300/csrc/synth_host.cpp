@@ -26,6 +26,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <atomic>
 #include <thread>
 #include <vector>
 
@@ -393,17 +394,21 @@ class Arena {
 };
 
 // Cached sorted-offset lists (they depend only on the box and the radius).
-const std::vector<int2>& cached_offsets(int w, int h, long long maxD2) {
+// Shared ownership: a caller keeps its list alive while other threads evict.
+std::shared_ptr<const std::vector<int2>> cached_offsets(int w, int h, long long maxD2) {
   static std::mutex mu;
-  static std::map<std::tuple<int, int, long long>, std::vector<int2>> cache;
-  std::lock_guard<std::mutex> lock(mu);
-  auto key = std::make_tuple(w, h, maxD2);
-  auto it = cache.find(key);
-  if (it == cache.end()) {
-    if (cache.size() > 16) cache.clear();
-    it = cache.emplace(key, sorted_offsets(w, h, maxD2)).first;
+  static std::map<std::tuple<int, int, long long>, std::shared_ptr<const std::vector<int2>>> cache;
+  const auto key = std::make_tuple(w, h, maxD2);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
   }
-  return it->second;
+  auto list = std::make_shared<const std::vector<int2>>(sorted_offsets(w, h, maxD2));
+  std::lock_guard<std::mutex> lock(mu);
+  if (cache.size() > 16) cache.clear();
+  cache.emplace(key, list);
+  return list;
 }
 
 struct RecordedState {
@@ -583,7 +588,8 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
   }
   const int mw = (int)std::min(tw, cw), mh = (int)std::min(th, ch);
   const long long maxD2 = replay ? LLONG_MAX : wave_radius2(mw, mh);
-  const std::vector<int2>& offs = cached_offsets(mw, mh, maxD2);
+  const auto offsHeld = cached_offsets(mw, mh, maxD2);
+  const std::vector<int2>& offs = *offsHeld;
 
   Arena ar(s);
   unsigned long long h2d = 0;
@@ -709,6 +715,16 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     wa.stageSrc = ar.alloc<int2>(ntargets);
     int2* dPass = ar.alloc<int2>(ntargets);
     int* dBandEnds = ar.alloc<int>(kMaxBands);
+    int* dBandPhased = ar.alloc<int>(kMaxBands);
+    // Visit stamps replace hasValue writes: a pixel has a value for batch b of
+    // pass 0 iff its stamp < b, and every target has one in later passes.
+    int* vis = ar.alloc<int>((size_t)tw * th);
+    CK(rs_vis_init(dp.pb.has, (int)(tw * th), vis, s));
+    launches++;
+    wa.pb.vis = vis;
+    // Stores go straight into the state unless the target wraps (tiling): then
+    // colour phases can meet across the seam, and results are staged.
+    wa.inPlace = (dp.pb.tileH || dp.pb.tileV) ? 0 : 1;
     int* batchStart = ar.alloc<int>((size_t)kMaxBands * k * k + 1);
     int* work = ar.alloc<int>(3 * (size_t)kMaxBands * k * k + 1 + ntargets);
     wa.targets = dPass;
@@ -734,24 +750,34 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
         for (unsigned r = 1; r <= refine; r++) bandEnds.push_back((int)((unsigned long long)end * r / refine));
       }
       const int nb = (int)bandEnds.size();
+      // Every band is split into colour phases.  (Leaving sparse pass-0 bands
+      // whole saves batches but costs energy: same-band targets then miss each
+      // other inside their wide sparse patches.)
+      std::vector<int> phased(nb, 1);
       CK(cudaMemcpyAsync(dBandEnds, bandEnds.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
-      h2d += nb * sizeof(int);
+      CK(cudaMemcpyAsync(dBandPhased, phased.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
+      h2d += 2 * nb * sizeof(int);
       // Bucket this pass's targets by (band, colour phase): targets of one
       // phase are at least k apart, farther than a dense patch reaches, so
       // the targets of one batch never read each other.
       CK(rs_prep_batches(dTargets, (int)ntargets, (int)tw, (int)end, randomOrder ? 1 : 0, wa.seed ^ 0x5bd1e995u,
-                         dBandEnds, nb, k, work, batchStart, dPass, s));
+                         dBandEnds, dBandPhased, nb, k, work, batchStart, dPass, pass == 0 ? vis : nullptr, s));
       launches += 4;
       const int nbatches = nb * k * k;
       wa.pass = (unsigned)pass;
       wa.sparse = (pass == 0 && sparseOk) ? 1 : 0;
       for (int b = 0; b < nbatches; b++) {
+        if (!phased[b / (k * k)] && b % (k * k)) continue;   // empty by construction
         wa.batch = b;
+        wa.visCur = pass == 0 ? b : 0x7ffffffe;
         if (opt.profile) prof.begin(s);
         CK(rs_launch_wave(wa, (int)opt.warpsPerBlock, s));
         if (opt.profile) prof.end(s);
-        CK(rs_launch_commit(wa, s));
-        launches += 2;
+        launches++;
+        if (!wa.inPlace) {
+          CK(rs_launch_commit(wa, s));
+          launches++;
+        }
       }
       CK(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(st.hostInts + 3, batchStart + nbatches, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -773,6 +799,8 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     for (unsigned i = 0; i < stats.passes; i++) stats.visits += stats.passLength[i];
     stats.evals = hc.evals;
     stats.terms = hc.terms;
+    CK(rs_vis_to_has(vis, (int)(tw * th), dp.pb.has, s));
+    launches++;
     if (opt.profile) {
       CK(cudaStreamSynchronize(s));
       stats.waveMs = prof.total();
@@ -922,7 +950,8 @@ int score_host(bool energyMode, const TImageSynthParameters* p, const TFormatInd
   const uint8_t* dT = ar.upload(target, tb, h2d);
   const uint8_t* dC = ar.upload(corpus, cbytes, h2d);
   const int mw = (int)std::min(tw, cw), mh = (int)std::min(th, ch);
-  const std::vector<int2>& offs = cached_offsets(mw, mh, LLONG_MAX);
+  const auto offsHeld = cached_offsets(mw, mh, LLONG_MAX);
+  const std::vector<int2>& offs = *offsHeld;
   DeviceProblem dp = make_problem(ar, s, *p, *f, dT, tw, th, dC, cw, ch, hasValue,
                                   reinterpret_cast<const int2*>(sourceOf), offs, LLONG_MAX, h2d, launches);
   rs::ScoreArgs sa{};
@@ -1122,6 +1151,43 @@ RS_EXPORT int imageSynth(ImageBuffer* img, ImageBuffer* mask, TImageFormat fmt, 
 RS_EXPORT int imageSynth2(ImageBuffer* img, ImageBuffer* mask, ImageBuffer* mask2, TImageFormat fmt,
                           TImageSynthParameters* params, void (*cb)(int, void*), void* ctx, int* cancel) {
   return imageSynthEx(img, mask, mask2, fmt, params, cb, ctx, cancel, nullptr, nullptr);
+}
+
+RS_EXPORT int imageSynthBatch(TResynthRequest* requests, unsigned int count, unsigned int concurrency,
+                              const TResynthOptions* options, TResynthStats* stats) {
+  if (!requests && count) return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  const auto t0 = std::chrono::steady_clock::now();
+  const TResynthOptions opt = options_or_default(options);
+  const unsigned workers = std::max(1u, std::min(count, concurrency ? concurrency : 8u));
+  std::vector<TResynthStats> per(count);
+  std::atomic<unsigned> next{0};
+  auto work = [&] {
+    for (unsigned i = next++; i < count; i = next++) {
+      TResynthRequest& r = requests[i];
+      r.result = imageSynthEx(r.image, r.mask, r.mask2, r.format, r.parameters, nullptr, nullptr, nullptr, &opt,
+                              &per[i]);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned w = 1; w < workers; w++) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  int rc = 0;
+  TResynthStats total{};
+  for (unsigned i = 0; i < count; i++) {
+    if (!rc && requests[i].result) rc = requests[i].result;
+    total.visits += per[i].visits;
+    total.evals += per[i].evals;
+    total.terms += per[i].terms;
+    total.launches += per[i].launches;
+    total.deviceMs += per[i].deviceMs;
+    total.h2dBytes += per[i].h2dBytes;
+    total.d2hBytes += per[i].d2hBytes;
+    total.passes = std::max(total.passes, per[i].passes);
+  }
+  total.totalMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = total;
+  return rc;
 }
 
 RS_EXPORT int engineDevice(const TImageSynthParameters* p, const TFormatIndices* f, unsigned char* dTarget,

@@ -22,6 +22,8 @@ struct Problem {
   uint32_t* tpx;              // target pixels (tw*th)
   uint32_t* tmap;             // target map channels (tw*th) or null
   uint8_t* has;               // hasValue (tw*th)
+  const int* vis;             // wavefront: visit stamp per pixel; a pixel has a value for batch b iff vis < b
+                              // (null: use has)
   int2* src;                  // sourceOf (tw*th)
   const uint32_t* cpx;        // corpus pixels (cw*ch)
   const uint32_t* cmap;       // corpus map channels (cw*ch) or null
@@ -72,6 +74,8 @@ struct WaveArgs {
   const int2* targets;           // this pass's targets, bucketed by batch
   const int* batchStart;         // device: batch boundaries
   int batch;
+  int visCur;                    // pixels with vis < visCur have values during this batch
+  int inPlace;                   // write results straight into the state (else stage for k_commit)
   int sparse;                    // allowed: patches from the valued list targets[0 .. b0)
   long long sparseLimit2;        // ... while b0 * b0 < sparseLimit2
   unsigned int trys;
@@ -115,6 +119,8 @@ cudaError_t rs_prep_corpus(const uint8_t* raw, int w, int h, int bpp, int alpha,
                            int2* points, int* count, cudaStream_t s);
 int rs_prep_scratch_ints(int w, int h);
 cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
-                            const int* dBandEnds, int nbands, int k, int* work, int* batchStart, int2* out,
-                            cudaStream_t s);
+                            const int* dBandEnds, const int* dBandPhased, int nbands, int k, int* work,
+                            int* batchStart, int2* out, int* vis, cudaStream_t s);
+cudaError_t rs_vis_init(const uint8_t* has, int npx, int* vis, cudaStream_t s);
+cudaError_t rs_vis_to_has(const int* vis, int npx, uint8_t* has, cudaStream_t s);
 }

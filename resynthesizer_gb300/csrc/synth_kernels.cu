@@ -12,11 +12,14 @@
 //   k_replay   one CTA visiting targets in the reference order (bit-exact
 //              sequential replay of lib/synthesize.h:426-642)
 //   k_wave     warp-per-target synthesis of one wavefront batch
-//   k_commit   applies a batch's staged results (setColor/setSourceOf/setHasValue)
+//   k_commit   applies a batch's staged results when they cannot be stored in
+//              place (tiled targets)
 //   k_frozen   frozen-state best fit over explicit candidate lists
 //   k_energy   full-patch metric at each target's source
 #include <climits>
 #include <cstdint>
+#include <map>
+#include <mutex>
 
 #include "synth_internal.h"
 
@@ -92,7 +95,7 @@ __device__ __forceinline__ void load_nb(const Problem& pb, Patch& P, int slot, i
 // prepare_neighbors for one target with one warp: the target itself first,
 // then the nearest sorted offsets whose point lies in (or wraps into) the
 // target image and has a value, until the patch limit.  Returns the count.
-__device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int lane) {
+__device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int lane, int visCur = 0) {
   if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
   int count = 1;
   const int limit = pb.patchLimit;
@@ -106,7 +109,7 @@ __device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int
       int qx = px + o.x, qy = py + o.y;
       if (wrap_or_clip(pb, qx, qy)) {
         qi = qy * pb.tw + qx;
-        ok = pb.has[qi] != 0;
+        ok = pb.vis ? pb.vis[qi] < visCur : pb.has[qi] != 0;
       }
     }
     const unsigned m = __ballot_sync(kFull, ok);
@@ -392,7 +395,8 @@ __device__ bool stage_words(uint32_t* dst, const uint32_t* src, unsigned words, 
     }
     __nanosleep(64);
   }
-  return ok;
+  // Every thread's wait is bounded; the CTA acts on one shared verdict.
+  return __syncthreads_and(ok) != 0;
 }
 
 // ------------------------------------------------------------------ frozen
@@ -700,6 +704,9 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   int2* prop = reinterpret_cast<int2*>(topk);
   __shared__ unsigned long long s_key[16];
   __shared__ int s_n[16], s_np[16], s_fast[16];
+  __shared__ unsigned s_better;
+  if (threadIdx.x == 0) s_better = 0;
+  __syncthreads();
   auto team_sync = [&]() {
     if (G == 1) __syncwarp();
     else asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(G * 32) : "memory");
@@ -712,7 +719,7 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
     const int pi = pos.y * pb.tw + pos.x;
     if (tw == 0) {
       const int n = sparse ? build_patch_sparse(pb, pos.x, pos.y, P, topk, a.targets, b0, lane)
-                           : build_patch_warp(pb, pos.x, pos.y, P, lane);
+                           : build_patch_warp(pb, pos.x, pos.y, P, lane, a.visCur);
       // linear offsets into the padded corpus; the fast path needs all within kPad
       int far = 0;
       for (int i = lane; i < n; i += 32) {
@@ -777,10 +784,23 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
         const int2 cur = pb.src[pi];
         if (cur.x != pt.x || cur.y != pt.y) out = pt;
       }
-      a.stageSrc[slot] = out;
+      if (a.inPlace) {
+        // No target of this batch reads another's state (visit stamps, colour
+        // phases), so the store (setColor + setSourceOf) happens right here.
+        if (out.x != -2) {
+          const uint32_t c = pb.cpx[out.y * pb.cw + out.x];
+          pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (c & 0xFFFFFF00u);
+          pb.src[pi] = out;
+          atomicAdd(&s_better, 1u);
+        }
+      } else {
+        a.stageSrc[slot] = out;
+      }
     }
     team_sync();
   }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_better) atomicAdd(&a.ctr->betters, s_better);
   unsigned long long tv = warp_sum_u64(terms), ev = warp_sum_u64(evals);
   if (lane == 0) {
     atomicAdd(&a.ctr->terms, tv);
@@ -807,7 +827,7 @@ __global__ void k_commit(WaveArgs a) {
       pb.src[pi] = s;
       better++;
     }
-    pb.has[pi] = 1;
+    if (!pb.vis) pb.has[pi] = 1;
   }
   for (int o = 16; o > 0; o >>= 1) better += __shfl_xor_sync(kFull, better, o);
   if ((threadIdx.x & 31) == 0 && better) atomicAdd(&a.ctr->betters, better);
@@ -862,13 +882,12 @@ int grid_for(int n, int perBlock, int maxBlocks) {
 }
 
 int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
+  static const int n = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
   return n;
 }
 
@@ -940,17 +959,25 @@ size_t wave_smem(const Problem& pb, bool smemc, int warps) {
 template <int NC, bool MAP, bool SMEMC>
 cudaError_t launch_wave_t(const WaveArgs& a, int warps, size_t smem, cudaStream_t s) {
   auto kern = k_wave<NC, MAP, SMEMC>;
+  // Per-instantiation launch configuration, shared by all host threads.
+  static std::mutex mu;
   static size_t configured = 0;
-  if (smem > configured) {
-    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = smem;
-  }
-  static int perSm = 0;
-  static size_t perSmFor = 0;
-  if (perSmFor != smem) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
-    perSmFor = smem;
+  static std::map<std::pair<size_t, int>, int> perSmCache;
+  int perSm = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (smem > configured) {
+      const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = smem;
+    }
+    auto it = perSmCache.find({smem, warps});
+    if (it == perSmCache.end()) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
+      perSmCache[{smem, warps}] = perSm;
+    } else {
+      perSm = it->second;
+    }
   }
   if (perSm < 1) return cudaErrorInvalidConfiguration;
   // Persistent grid: the batch size is only known on the device.

@@ -164,7 +164,8 @@ __device__ __forceinline__ int warp_bump(int* counter, int key) {
 }
 
 __global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
-                             const int* bandEnds, int nbands, int k, int* keys, int* hist) {
+                             const int* bandEnds, const int* bandPhased, int nbands, int k, int* keys, int* hist,
+                             int* vis) {
   const int stride = gridDim.x * blockDim.x;
   const int limit = (n + stride - 1) / stride * stride;   // whole warps iterate together
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < limit; t += stride) {
@@ -177,9 +178,11 @@ __global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, in
       if (rank < endRank) {
         int band = 0;
         while (band < nbands - 1 && rank >= bandEnds[band]) band++;
-        key = band * k * k + (p.y % k) * k + (p.x % k);
+        key = band * k * k + (bandPhased[band] ? (p.y % k) * k + (p.x % k) : 0);
       }
       keys[t] = key;
+      // pass 0: the pixel gets its value in batch `key`
+      if (vis && key >= 0) vis[p.y * tw + p.x] = key;
     }
     warp_bump(hist, key);
   }
@@ -241,17 +244,43 @@ extern "C" int rs_prep_scratch_ints(int w, int h) { return 2 * blocks_for(w * h,
 // batchStart[b+1]) are the targets of batch b = band * k * k + phase.
 // work: 3 * nkeys + 1 + n ints.
 extern "C" cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder,
-                                       uint32_t seed, const int* dBandEnds, int nbands, int k, int* work,
-                                       int* batchStart, int2* out, cudaStream_t s) {
+                                       uint32_t seed, const int* dBandEnds, const int* dBandPhased, int nbands,
+                                       int k, int* work, int* batchStart, int2* out, int* vis, cudaStream_t s) {
   const int nkeys = nbands * k * k;
   int* hist = work;
   int* cursor = work + nkeys;
   int* keys = work + 2 * nkeys + 1;
   cudaMemsetAsync(hist, 0, sizeof(int) * nkeys, s);
   const int g = std::min(blocks_for(n, 256), 1184);
-  k_batch_keys<<<g, 256, 0, s>>>(targets, n, tw, endRank, randomOrder, seed, dBandEnds, nbands, k, keys, hist);
+  k_batch_keys<<<g, 256, 0, s>>>(targets, n, tw, endRank, randomOrder, seed, dBandEnds, dBandPhased, nbands, k,
+                                 keys, hist, vis);
   k_scan<<<1, kThreads, 0, s>>>(hist, nkeys, batchStart);
   k_copy_int<<<blocks_for(nkeys, 256), 256, 0, s>>>(batchStart, cursor, nkeys);
   k_scatter<<<g, 256, 0, s>>>(targets, n, keys, cursor, out);
+  return cudaGetLastError();
+}
+
+namespace rs {
+namespace {
+// Visit stamps before pass 0: -1 for pixels that have a value from the start
+// (context), INT_MAX for the rest; targets get their batch index in pass 0.
+__global__ void k_vis_init(const uint8_t* has, int npx, int* vis) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x)
+    vis[i] = has[i] ? -1 : 0x7fffffff;
+}
+__global__ void k_vis_to_has(const int* vis, int npx, uint8_t* has) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x)
+    has[i] = vis[i] != 0x7fffffff ? 1 : 0;
+}
+}  // namespace
+}  // namespace rs
+
+extern "C" cudaError_t rs_vis_init(const uint8_t* has, int npx, int* vis, cudaStream_t s) {
+  k_vis_init<<<std::min(blocks_for(npx, 256), 2048), 256, 0, s>>>(has, npx, vis);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_vis_to_has(const int* vis, int npx, uint8_t* has, cudaStream_t s) {
+  k_vis_to_has<<<std::min(blocks_for(npx, 256), 2048), 256, 0, s>>>(vis, npx, has);
   return cudaGetLastError();
 }
