@@ -904,6 +904,56 @@ int image_synth_impl(ImageBuffer* img, ImageBuffer* mask, ImageBuffer* mask2, TI
   if (rc0) return rc0;
   const unsigned bpp = countPixelelsPerPixelForFormat(fmt), w = img->width, h = img->height;
   const unsigned d = bpp + 1;
+  int zero0 = 0;
+  if (!cancel) cancel = &zero0;
+  if (opt.mode != RESYNTH_MODE_REPLAY && (params->matchContextType == 0 || params->matchContextType == 1)) {
+    // Device path: the adaption runs on the GPU from one upload of the
+    // caller's buffers; only the reference's up-front checks use the host.
+    if (params->patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+    ImageBuffer* cm = mask2 ? mask2 : mask;
+    bool anyTarget = false, anyCorpus = false;
+    for (unsigned y = 0; y < h && !anyTarget; y++)
+      for (unsigned x = 0; x < w && !anyTarget; x++) anyTarget = mask->data[y * mask->rowBytes + x] != 0;
+    if (!anyTarget) return IMAGE_SYNTH_ERROR_EMPTY_TARGET;
+    for (unsigned y = 0; y < h && !anyCorpus; y++)
+      for (unsigned x = 0; x < w && !anyCorpus; x++) {
+        const uint8_t m = cm->data[y * cm->rowBytes + x];
+        const uint8_t cmask = mask2 ? m : (uint8_t)~m;
+        anyCorpus = cmask == 0xFF && (!f.isAlphaSource || img->data[y * img->rowBytes + (size_t)x * bpp + f.alpha_bip - 1] != 0);
+      }
+    if (!anyCorpus) return IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
+    Stream& st = thread_stream();
+    cudaStream_t s = st.s;
+    Arena ar(s);
+    const size_t imgBytes = img->rowBytes * (h - 1) + (size_t)w * bpp;
+    const size_t mBytes = mask->rowBytes * (h - 1) + w;
+    uint8_t* dImg = ar.alloc<uint8_t>(img->rowBytes * h);
+    uint8_t* dMask = ar.alloc<uint8_t>(mask->rowBytes * h);
+    uint8_t* dMask2 = mask2 ? ar.alloc<uint8_t>(mask2->rowBytes * h) : nullptr;
+    CK(cudaMemcpyAsync(dImg, img->data, imgBytes, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dMask, mask->data, mBytes, cudaMemcpyHostToDevice, s));
+    stats.h2dBytes += imgBytes + mBytes;
+    if (mask2) {
+      const size_t m2Bytes = mask2->rowBytes * (h - 1) + w;
+      CK(cudaMemcpyAsync(dMask2, mask2->data, m2Bytes, cudaMemcpyHostToDevice, s));
+      stats.h2dBytes += m2Bytes;
+    }
+    uint8_t* dT = ar.alloc<uint8_t>((size_t)w * h * d);
+    uint8_t* dC = ar.alloc<uint8_t>((size_t)w * h * d);
+    CK(rs_adapt(dImg, img->rowBytes, dMask, mask->rowBytes, dMask2, mask2 ? mask2->rowBytes : 0, (int)w, (int)h,
+                (int)bpp, dT, dC, s));
+    const int rc = run_engine_device(*params, f, dT, w, h, dC, w, h, nullptr, s, cb, ctx, cancel, opt, stats);
+    stats.launches += 1;
+    if (rc) return rc;
+    if (!*cancel) {
+      CK(rs_unadapt(dT, (int)w, (int)h, (int)bpp, dImg, img->rowBytes, s));
+      CK(cudaMemcpyAsync(img->data, dImg, imgBytes, cudaMemcpyDeviceToHost, s));
+      stats.d2hBytes += imgBytes;
+      stats.launches += 1;
+    }
+    CK(cudaStreamSynchronize(s));
+    return 0;
+  }
   std::vector<uint8_t> tgt((size_t)w * h * d), cor((size_t)w * h * d);
   ImageBuffer* cm = mask2 ? mask2 : mask;
   for (unsigned y = 0; y < h; y++) {
@@ -919,8 +969,6 @@ int image_synth_impl(ImageBuffer* img, ImageBuffer* mask, ImageBuffer* mask2, TI
       memcpy(c + 1, srow + (size_t)x * bpp, bpp);
     }
   }
-  int zero = 0;
-  if (!cancel) cancel = &zero;
   const int rc = run_engine_host(*params, f, tgt.data(), w, h, cor.data(), w, h, cb, ctx, cancel, opt, stats);
   if (!rc && !*cancel) {
     for (unsigned y = 0; y < h; y++) {

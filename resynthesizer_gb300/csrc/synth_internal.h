@@ -121,6 +121,9 @@ int rs_prep_scratch_ints(int w, int h);
 cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
                             const int* dBandEnds, const int* dBandPhased, int nbands, int k, int* work,
                             int* batchStart, int2* out, int* vis, cudaStream_t s);
+cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, size_t maskRow, const uint8_t* mask2,
+                     size_t mask2Row, int w, int h, int bpp, uint8_t* target, uint8_t* corpus, cudaStream_t s);
+cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow, cudaStream_t s);
 cudaError_t rs_vis_init(const uint8_t* has, int npx, int* vis, cudaStream_t s);
 cudaError_t rs_vis_to_has(const int* vis, int npx, uint8_t* has, cudaStream_t s);
 }

@@ -284,3 +284,51 @@ extern "C" cudaError_t rs_vis_to_has(const int* vis, int npx, uint8_t* has, cuda
   k_vis_to_has<<<std::min(blocks_for(npx, 256), 2048), 256, 0, s>>>(vis, npx, has);
   return cudaGetLastError();
 }
+
+// ---------------------------------------------------------- simple-API adapters
+// adaptSimpleAPI / adaptSimpleAPI2 (lib/adaptSimple.h:260-354) on the device:
+// the caller's row-padded image and mask(s) become the interleaved target
+// pixmap [mask][pixelels] and corpus pixmap [~mask or mask2][pixelels].
+namespace rs {
+namespace {
+__global__ void k_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, size_t maskRow, const uint8_t* mask2,
+                        size_t mask2Row, int w, int h, int bpp, uint8_t* target, uint8_t* corpus) {
+  const int d = bpp + 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w * h; i += gridDim.x * blockDim.x) {
+    const int x = i % w, y = i / w;
+    const uint8_t* s = img + (size_t)y * imgRow + (size_t)x * bpp;
+    uint8_t* t = target + (size_t)i * d;
+    uint8_t* c = corpus + (size_t)i * d;
+    const uint8_t m = mask[(size_t)y * maskRow + x];
+    t[0] = m;
+    c[0] = mask2 ? mask2[(size_t)y * mask2Row + x] : (uint8_t)~m;
+    for (int k = 0; k < bpp; k++) t[1 + k] = c[1 + k] = s[k];
+  }
+}
+// antiAdaptImage (lib/adaptSimple.h:110-168): every pixel's pixelels back
+// into the row-padded image (only target colours can have changed).
+__global__ void k_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow) {
+  const int d = bpp + 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w * h; i += gridDim.x * blockDim.x) {
+    const int x = i % w, y = i / w;
+    uint8_t* o = img + (size_t)y * imgRow + (size_t)x * bpp;
+    const uint8_t* t = target + (size_t)i * d;
+    for (int k = 0; k < bpp; k++) o[k] = t[1 + k];
+  }
+}
+}  // namespace
+}  // namespace rs
+
+extern "C" cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, size_t maskRow,
+                                const uint8_t* mask2, size_t mask2Row, int w, int h, int bpp, uint8_t* target,
+                                uint8_t* corpus, cudaStream_t s) {
+  k_adapt<<<std::min(blocks_for(w * h, 256), 4096), 256, 0, s>>>(img, imgRow, mask, maskRow, mask2, mask2Row, w, h,
+                                                                   bpp, target, corpus);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow,
+                                  cudaStream_t s) {
+  k_unadapt<<<std::min(blocks_for(w * h, 256), 4096), 256, 0, s>>>(target, w, h, bpp, img, imgRow);
+  return cudaGetLastError();
+}
