@@ -277,6 +277,14 @@ int imageSynthBatch(TResynthRequest *requests, unsigned int count, unsigned int 
 /* Text of the last error on this thread ("" if none). */
 const char *resynthLastError(void);
 
+/* ------------------------------------------------------ learned proposals */
+
+/* No counterpart in the reference.  Test entry of the tensor-core GEMM that
+ * the proposal network runs on: D[M x N] = bf16(A)[M x K] . bf16(B)[N x K]^T
+ * with fp32 accumulation (A, B, D host row-major; inputs rounded to nearest
+ * even bf16).  N must be a multiple of 32. */
+int resynthTcGemm(const float *A, const float *B, int M, int N, int K, float *D);
+
 #ifdef __cplusplus
 }
 #endif

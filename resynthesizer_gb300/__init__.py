@@ -130,6 +130,7 @@ def lib() -> C.CDLL:
         L.set_bytemap.argtypes = [P(Map), C.c_ubyte]
         L.invert_bytemap.argtypes = [P(Map)]
         L.interleave_mask.argtypes = [P(Map), P(Map)]
+        L.resynthTcGemm.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp]
         _lib = L
     return _lib
 
@@ -325,3 +326,16 @@ def image_synth_batch(items, opts: Options | None = None, concurrency: int = 8):
     st = Stats()
     rc = lib().imageSynthBatch(reqs, len(items), concurrency, C.byref(opts) if opts else None, C.byref(st))
     return rc, [k[0] for k in keep], [reqs[i].result for i in range(len(items))], st.as_dict()
+
+
+def tc_gemm(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """D = bf16(a) . bf16(b)^T on the tensor cores (fp32 accumulation)."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    m, k = a.shape
+    n = b.shape[0]
+    d = np.zeros((m, n), np.float32)
+    rc = lib().resynthTcGemm(_vp(a), _vp(b), m, n, k, _vp(d))
+    if rc:
+        raise RuntimeError(f"resynthTcGemm rc={rc}: {last_error()}")
+    return d
