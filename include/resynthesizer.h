@@ -138,6 +138,10 @@ typedef enum {
   RESYNTH_MODE_REPLAY = 1
 } TResynthMode;
 
+/* Opaque objects of the learned proposal network (declared at the end). */
+typedef struct TResynthNet TResynthNet;
+typedef struct TResynthPairs TResynthPairs;
+
 typedef struct {
   int mode;                   /* TResynthMode */
   unsigned int seed;          /* wavefront probe RNG seed (0 = 1198472) */
@@ -149,6 +153,10 @@ typedef struct {
   unsigned int phaseSide;     /* wavefront: k of the k x k colour phases (0 = from the patch radius, 1 = none) */
   unsigned int bandGrowth;    /* wavefront: pass-0 band growth in percent for random orders (0 = 200) */
   unsigned int minPasses;     /* wavefront: run at least this many passes (0 = the reference's stop rule only) */
+  TResynthNet *net;           /* wavefront: score this network's proposals at every visit (NULL = none) */
+  unsigned int proposals;     /* wavefront: how many of the network's 16 offsets are scored (0 = none) */
+  TResynthPairs *dumpPairs;   /* wavefront: append (context, final source) training pairs at the end */
+  unsigned int dumpStride;    /* every dumpStride-th target of the visit order gives a pair (0 = 16) */
 } TResynthOptions;
 
 typedef struct {
@@ -284,6 +292,67 @@ const char *resynthLastError(void);
  * with fp32 accumulation (A, B, D host row-major; inputs rounded to nearest
  * even bf16).  N must be a multiple of 32. */
 int resynthTcGemm(const float *A, const float *B, int M, int N, int K, float *D);
+
+/* No counterpart in the reference.  The proposal network reads an 11 x 11
+ * context around a target pixel and emits 16 source offsets; in wavefront
+ * mode (TResynthOptions.net) they join each visit's candidates next to the
+ * neighbours' continuations and the random probes (lib/synthesize.h:536-604)
+ * and are scored by the same exact metric, so the plain search stays both
+ * fallback and judge.
+ *
+ * Context: 11 x 11 pixels x 16 bf16 channels, row-major (y, x, channel),
+ * centred on the target.  Channels 0-2 colour (grey repeated) as v/255 - 0.5,
+ * channel 3 = 1 where the pixel has a value (colours are 0 where it has
+ * none), channel 4 = first map channel as m/255 - 0.5 (0 without maps),
+ * channels 5-15 = 0; pixels outside the image are all 0.
+ * Network: four 3x3 convolutions of 32 channels with ReLU (11 -> 9 -> 7 -> 5
+ * -> 3), then a 3x3 convolution to 32 outputs = 16 x (dx, dy) in units of 64
+ * pixels.  BF16 weights and activations, fp32 accumulation on the tensor
+ * cores.  Parameters (fp32, resynthNetParamCount() of them): for each layer
+ * W [32 x 9*Cin] (column (ky*3 + kx)*Cin + c, Cin = 16 then 32) then b [32].
+ * Training minimises the relaxed multiple-choice loss: the offset nearest the
+ * label (source - target, / 64, clipped to +-16) weighs 0.95, each other
+ * 0.05/15, loss = mean of sum_k w_k |o_k - label|^2, with Adam. */
+unsigned int resynthNetParamCount(void);
+
+/* A network with He-normal weights drawn from `seed`, on the current device.
+ * NULL on failure (reason in resynthLastError()). */
+TResynthNet *resynthNetCreate(unsigned int seed);
+void resynthNetDestroy(TResynthNet *net);
+int resynthNetGetParams(TResynthNet *net, float *params);
+int resynthNetSetParams(TResynthNet *net, const float *params);
+
+/* Outputs [n x 32] for contexts [n x 11 x 11 x 16] (bf16 bits), host
+ * buffers.  path 0 = the fused inference kernel, 1 = the training kernels. */
+int resynthNetForward(TResynthNet *net, const unsigned short *contexts, unsigned int n, float *out, int path);
+
+/* Loss and its gradient w.r.t. the parameters (resynthNetParamCount() floats)
+ * for contexts [n x 11 x 11 x 16] and labels [n x 2]; host buffers. */
+int resynthNetGradients(TResynthNet *net, const unsigned short *contexts, const float *labels, unsigned int n,
+                        float *gradient, float *loss);
+
+typedef struct {
+  unsigned int steps;          /* Adam steps (0 = 2000) */
+  unsigned int batch;          /* pairs per step (0 = 512) */
+  float learningRate;          /* 0 = 1e-3 */
+  unsigned int seed;           /* minibatch sampling */
+} TResynthTrainOptions;
+
+/* Trains on the pairs with the tensor-core forward and backward kernels.
+ * lossOut (may be NULL) receives the mean loss of the last tenth of the steps. */
+int resynthNetTrain(TResynthNet *net, TResynthPairs *pairs, const TResynthTrainOptions *options, float *lossOut);
+
+/* Device-resident store of training pairs (context, label). */
+TResynthPairs *resynthPairsCreate(unsigned int capacity);
+void resynthPairsDestroy(TResynthPairs *pairs);
+unsigned int resynthPairsCount(const TResynthPairs *pairs);
+/* Appends n host pairs (contexts as above, labels [n x 2] in units of 64 px);
+ * returns the number stored (the store keeps its first `capacity` pairs). */
+unsigned int resynthPairsAdd(TResynthPairs *pairs, const unsigned short *contexts, const float *labels,
+                             unsigned int n);
+/* Copies pairs [first, first + n) to host buffers (either may be NULL). */
+int resynthPairsRead(const TResynthPairs *pairs, unsigned int first, unsigned int n, unsigned short *contexts,
+                     float *labels);
 
 #ifdef __cplusplus
 }

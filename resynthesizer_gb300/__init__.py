@@ -58,7 +58,12 @@ class Map(C.Structure):
 class Options(C.Structure):
     _fields_ = [("mode", C.c_int), ("seed", C.c_uint), ("firstBatch", C.c_uint), ("refineBatches", C.c_uint),
                 ("warpsPerBlock", C.c_uint), ("recordState", C.c_int), ("profile", C.c_int),
-                ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint)]
+                ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint),
+                ("net", C.c_void_p), ("proposals", C.c_uint), ("dumpPairs", C.c_void_p), ("dumpStride", C.c_uint)]
+
+
+class TrainOptions(C.Structure):
+    _fields_ = [("steps", C.c_uint), ("batch", C.c_uint), ("learningRate", C.c_float), ("seed", C.c_uint)]
 
 
 class Request(C.Structure):
@@ -131,6 +136,23 @@ def lib() -> C.CDLL:
         L.invert_bytemap.argtypes = [P(Map)]
         L.interleave_mask.argtypes = [P(Map), P(Map)]
         L.resynthTcGemm.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp]
+        L.resynthNetParamCount.restype = u
+        L.resynthNetCreate.argtypes = [u]
+        L.resynthNetCreate.restype = vp
+        L.resynthNetDestroy.argtypes = [vp]
+        L.resynthNetGetParams.argtypes = [vp, vp]
+        L.resynthNetSetParams.argtypes = [vp, vp]
+        L.resynthNetForward.argtypes = [vp, vp, u, vp, C.c_int]
+        L.resynthNetGradients.argtypes = [vp, vp, vp, u, vp, P(C.c_float)]
+        L.resynthNetTrain.argtypes = [vp, vp, P(TrainOptions), P(C.c_float)]
+        L.resynthPairsCreate.argtypes = [u]
+        L.resynthPairsCreate.restype = vp
+        L.resynthPairsDestroy.argtypes = [vp]
+        L.resynthPairsCount.argtypes = [vp]
+        L.resynthPairsCount.restype = u
+        L.resynthPairsAdd.argtypes = [vp, vp, vp, u]
+        L.resynthPairsAdd.restype = u
+        L.resynthPairsRead.argtypes = [vp, u, u, vp, vp]
         _lib = L
     return _lib
 
@@ -157,7 +179,8 @@ def format_indices(colors, mapColors=0, alphaTarget=0, alphaSource=0, isMap=0) -
 
 
 def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, recordState=0,
-            profile=0, phaseSide=0, bandGrowth=0, minPasses=0) -> Options:
+            profile=0, phaseSide=0, bandGrowth=0, minPasses=0, net=None, proposals=0, dump=None,
+            dumpStride=0) -> Options:
     o = Options()
     lib().resynthDefaultOptions(C.byref(o))
     if mode is not None:
@@ -165,6 +188,10 @@ def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, r
     o.seed, o.firstBatch, o.refineBatches, o.warpsPerBlock, o.recordState, o.profile = (
         seed, firstBatch, refineBatches, warpsPerBlock, recordState, profile)
     o.phaseSide, o.bandGrowth, o.minPasses = phaseSide, bandGrowth, minPasses
+    o.net = net.handle if net is not None else None
+    o.proposals = proposals if net is not None else 0
+    o.dumpPairs = dump.handle if dump is not None else None
+    o.dumpStride = dumpStride
     return o
 
 
@@ -339,3 +366,105 @@ def tc_gemm(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     if rc:
         raise RuntimeError(f"resynthTcGemm rc={rc}: {last_error()}")
     return d
+
+
+# ------------------------------------------------------- learned proposals
+
+CTX_SHAPE = (11, 11, 16)
+
+
+class Net:
+    """The proposal network (resynthNetCreate ... resynthNetDestroy)."""
+
+    def __init__(self, seed: int = 1):
+        self.handle = lib().resynthNetCreate(seed)
+        if not self.handle:
+            raise RuntimeError(f"resynthNetCreate: {last_error()}")
+
+    def close(self):
+        if self.handle:
+            lib().resynthNetDestroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def param_count() -> int:
+        return int(lib().resynthNetParamCount())
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        _check(lib().resynthNetGetParams(self.handle, _vp(p)), "resynthNetGetParams")
+        return p
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.param_count()
+        _check(lib().resynthNetSetParams(self.handle, _vp(p)), "resynthNetSetParams")
+
+    def forward(self, contexts: np.ndarray, path: int = 0) -> np.ndarray:
+        """contexts: uint16 bf16 bits [n, 11, 11, 16] -> outputs [n, 32]."""
+        x = np.ascontiguousarray(contexts, np.uint16)
+        n = x.shape[0]
+        out = np.zeros((n, 32), np.float32)
+        _check(lib().resynthNetForward(self.handle, _vp(x), n, _vp(out), path), "resynthNetForward")
+        return out
+
+    def gradients(self, contexts: np.ndarray, labels: np.ndarray):
+        x = np.ascontiguousarray(contexts, np.uint16)
+        y = np.ascontiguousarray(labels, np.float32)
+        g = np.zeros(self.param_count(), np.float32)
+        loss = C.c_float(0)
+        _check(lib().resynthNetGradients(self.handle, _vp(x), _vp(y), x.shape[0], _vp(g), C.byref(loss)),
+               "resynthNetGradients")
+        return float(loss.value), g
+
+    def train(self, pairs: "Pairs", steps=2000, batch=512, lr=1e-3, seed=0) -> float:
+        o = TrainOptions(steps, batch, lr, seed)
+        loss = C.c_float(0)
+        _check(lib().resynthNetTrain(self.handle, pairs.handle, C.byref(o), C.byref(loss)), "resynthNetTrain")
+        return float(loss.value)
+
+
+class Pairs:
+    """Device-resident training pairs (resynthPairsCreate ... resynthPairsDestroy)."""
+
+    def __init__(self, capacity: int):
+        self.handle = lib().resynthPairsCreate(capacity)
+        if not self.handle:
+            raise RuntimeError(f"resynthPairsCreate: {last_error()}")
+
+    def close(self):
+        if self.handle:
+            lib().resynthPairsDestroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return int(lib().resynthPairsCount(self.handle))
+
+    def add(self, contexts: np.ndarray, labels: np.ndarray) -> int:
+        x = np.ascontiguousarray(contexts, np.uint16)
+        y = np.ascontiguousarray(labels, np.float32)
+        return int(lib().resynthPairsAdd(self.handle, _vp(x), _vp(y), x.shape[0]))
+
+    def read(self, first=0, n=None):
+        n = len(self) - first if n is None else n
+        x = np.zeros((n,) + CTX_SHAPE, np.uint16)
+        y = np.zeros((n, 2), np.float32)
+        _check(lib().resynthPairsRead(self.handle, first, n, _vp(x), _vp(y)), "resynthPairsRead")
+        return x, y
+
+
+def _check(rc, what):
+    if rc:
+        raise RuntimeError(f"{what} rc={rc}: {last_error()}")

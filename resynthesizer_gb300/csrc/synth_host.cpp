@@ -729,6 +729,14 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     int* work = ar.alloc<int>(3 * (size_t)kMaxBands * k * k + 1 + ntargets);
     wa.targets = dPass;
     wa.batchStart = batchStart;
+    // Proposal network: run once per band over the band's targets, with the
+    // context the band starts from; its offsets join every visit's candidates.
+    const TResynthNet* net = opt.net && opt.proposals ? opt.net : nullptr;
+    int2* props = nullptr;
+    if (net) {
+      props = ar.alloc<int2>((size_t)ntargets * 16);
+      wa.nprop = (int)std::min(16u, opt.proposals);
+    }
     rs::Counters& hc = *st.hostCtr;
     LaunchTimer prof;
     for (int pass = 0; pass < rs::kPasses; pass++) {
@@ -768,6 +776,15 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       wa.sparse = (pass == 0 && sparseOk) ? 1 : 0;
       for (int b = 0; b < nbatches; b++) {
         if (!phased[b / (k * k)] && b % (k * k)) continue;   // empty by construction
+        if (net && b % (k * k) == 0) {
+          const int band = b / (k * k);
+          const int count = bandEnds[band] - (band ? bandEnds[band - 1] : 0);
+          CK(rs_net_propose(net, wa.pb, dPass, batchStart, b, b + k * k, count, pass == 0 ? b : 0x7ffffffe, props,
+                            &ctr->error, s));
+          launches++;
+          wa.props = props;
+          wa.propBatch0 = b;
+        }
         wa.batch = b;
         wa.visCur = pass == 0 ? b : 0x7ffffffe;
         if (opt.profile) prof.begin(s);
@@ -799,6 +816,10 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     for (unsigned i = 0; i < stats.passes; i++) stats.visits += stats.passLength[i];
     stats.evals = hc.evals;
     stats.terms = hc.terms;
+    if (opt.dumpPairs) {
+      CK(rs_net_dump(opt.dumpPairs, wa.pb, dTargets, (int)ntargets, opt.dumpStride, s));
+      launches++;
+    }
     CK(rs_vis_to_has(vis, (int)(tw * th), dp.pb.has, s));
     launches++;
     if (opt.profile) {

@@ -83,6 +83,9 @@ struct WaveArgs {
   int2* stageSrc;                // per-batch-slot new source, (-2, -2) = unchanged
   Counters* ctr;
   const volatile int* abortFlag; // host-mapped; nonzero stops the batch
+  const int2* props;             // proposal network's sources, 16 per target of the band, or null
+  int nprop;                     // how many of each target's 16 are scored
+  int propBatch0;                // the band's first batch: props index = t - batchStart[propBatch0]
 };
 
 // Frozen-state scoring and energy.
@@ -126,4 +129,14 @@ cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, siz
 cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow, cudaStream_t s);
 cudaError_t rs_vis_init(const uint8_t* has, int npx, int* vis, cudaStream_t s);
 cudaError_t rs_vis_to_has(const int* vis, int npx, uint8_t* has, cudaStream_t s);
+}
+
+// Proposal network (proposal_net.cu).
+struct TResynthNet;
+struct TResynthPairs;
+extern "C" {
+cudaError_t rs_net_propose(const TResynthNet* net, const rs::Problem& pb, const int2* targets, const int* batchStart,
+                           int batch0, int batch1, int count, int visCur, int2* props, unsigned* err, cudaStream_t s);
+cudaError_t rs_net_dump(TResynthPairs* pairs, const rs::Problem& pb, const int2* targets, int ntargets, unsigned stride,
+                        cudaStream_t s);
 }

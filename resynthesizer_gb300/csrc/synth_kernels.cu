@@ -645,9 +645,10 @@ struct WaveSmem {
 };
 
 // One wavefront batch: a warp per target.  Candidates are the deduplicated
-// in-corpus continuations of the patch's sources followed by `trys`
-// counter-based random probes; the best (first strict minimum) different
-// source is staged for k_commit.
+// in-corpus continuations of the patch's sources, then (with a proposal
+// network) the network's proposals, then `trys` counter-based random probes;
+// the best (first strict minimum) different source is stored in place, or
+// staged for k_commit when the target wraps.
 template <int NC, bool MAP, bool SMEMC>
 __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -758,16 +759,25 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
     team_sync();
     const int n = s_n[lead], np = s_np[lead];
     const bool fast = s_fast[lead] != 0;
-    const int ncand = np + (int)a.trys;
+    // Candidates: continuations, then the network's proposals (an invalid
+    // one is replaced by an extra probe), then the random probes.
+    const int nprop = a.props ? a.nprop : 0;
+    const int ncand = np + nprop + (int)a.trys;
     const uint32_t pbase = probe_base(a.seed, a.pass, (uint32_t)pi);
+    const int2* myProps = nprop ? a.props + (size_t)(t - a.batchStart[a.propBatch0]) * 16 : nullptr;
+    auto cand = [&](int k) -> int2 {
+      if (k < np) return prop[k];
+      if (k < np + nprop) {
+        const int2 c = myProps[k - np];
+        return corpus_ok(pb, cv, c) ? c : probe_point(pb, pbase, a.trys + (uint32_t)(k - np));
+      }
+      return probe_point(pb, pbase, (uint32_t)(k - np - nprop));
+    };
     // Warp tw of the team scores candidates tw, tw + G, tw + 2G, ...
     const int nloc = ncand > tw ? (ncand - tw + G - 1) / G : 0;
     uint32_t bv;
     int bi;
-    auto get = [&](int j) {
-      const int k = tw + j * G;
-      return k < np ? prop[k] : probe_point(pb, pbase, (uint32_t)(k - np));
-    };
+    auto get = [&](int j) { return cand(tw + j * G); };
     if (fast)
       score_warp<NC, MAP, true>(pb, cv, ct, mt, P, n, nloc, get, lane, bv, bi, terms, evals);
     else
@@ -780,7 +790,7 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
       int2 out = make_int2(-2, -2);
       if (best != ~0ull) {
         const int k = (int)(best & 0xffffffffu);
-        const int2 pt = k < np ? prop[k] : probe_point(pb, pbase, (uint32_t)(k - np));
+        const int2 pt = cand(k);
         const int2 cur = pb.src[pi];
         if (cur.x != pt.x || cur.y != pt.y) out = pt;
       }

@@ -32,3 +32,155 @@ def test_tc_gemm_matches_fp32(m, n, k):
     ref = bf16(a).astype(np.float64) @ bf16(b).astype(np.float64).T
     # fp32 accumulation of k products of bf16 values: relative error ~ k * 2^-24
     np.testing.assert_allclose(d, ref, rtol=1e-4, atol=1e-4 * np.sqrt(k))
+
+
+# ------------------------------------------------------------ the network
+
+import proposal_net as N   # noqa: E402
+
+
+def _contexts(n, seed):
+    """Contexts with the engine's channel structure: colours where valued, a
+    has-value channel, a map channel, zeros elsewhere."""
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 11, 11, 16), np.float32)
+    has = rng.random((n, 11, 11)) < 0.6
+    x[..., 0:3] = (rng.integers(0, 256, (n, 11, 11, 3)) / np.float32(255) - 0.5) * has[..., None]
+    x[..., 3] = has
+    x[..., 4] = rng.integers(0, 256, (n, 11, 11)) / np.float32(255) - 0.5
+    return N.bf16_bits(x)
+
+
+@pytest.fixture(scope="module")
+def net():
+    n = R.Net(seed=3)
+    yield n
+    n.close()
+
+
+@pytest.mark.parametrize("n", [1, 37, 300])
+@pytest.mark.parametrize("path", [0, 1])
+def test_net_forward_matches_oracle(net, n, path):
+    theta = net.get_params()
+    x = _contexts(n, seed=n)
+    out = net.forward(x, path=path)
+    ref, _ = N.forward(theta, N.bits_to_float(x))
+    # bf16 activations: a rounding flip between fp32 (GPU) and float64 sums
+    # moves an output by ~2^-8 of its scale
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(out, ref, rtol=2e-2, atol=2e-2 * scale)
+    assert np.abs(out - ref).mean() < 2e-3 * scale
+
+
+def test_net_paths_agree(net):
+    x = _contexts(200, seed=9)
+    a, b = net.forward(x, path=0), net.forward(x, path=1)
+    np.testing.assert_allclose(a, b, rtol=1e-2, atol=1e-2 * np.abs(b).max())
+
+
+@pytest.mark.parametrize("n", [5, 64])
+def test_net_gradients_match_oracle(net, n):
+    theta = net.get_params()
+    x = _contexts(n, seed=100 + n)
+    labels = np.random.default_rng(n).uniform(-2, 2, (n, 2)).astype(np.float32)
+    loss, g = net.gradients(x, labels)
+    ref_loss, ref_g = N.loss_and_grad(theta, N.bits_to_float(x), labels)
+    assert abs(loss - ref_loss) <= 1e-3 * abs(ref_loss) + 1e-6
+    o = 0
+    for cin, _ in N.LAYERS:
+        for size in (32 * 9 * cin, 32):
+            a, b = g[o:o + size], ref_g[o:o + size]
+            o += size
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+            assert rel < 2e-2, (o, rel)
+
+
+def test_net_training_reduces_loss():
+    # labels that are a function of the context: the mean of colour 0 over
+    # the valued pixels and the valued fraction
+    n = 4096
+    x = _contexts(n, seed=7)
+    xf = N.bits_to_float(x)
+    has = xf[..., 3]
+    lab = np.stack([4 * (xf[..., 0] * has).sum((1, 2)) / np.maximum(has.sum((1, 2)), 1),
+                    4 * has.mean((1, 2)) - 2], -1).astype(np.float32)
+    net = R.Net(seed=11)
+    pairs = R.Pairs(n)
+    assert pairs.add(x, lab) == n and len(pairs) == n
+    rx, ry = pairs.read(10, 5)
+    assert np.array_equal(rx, x[10:15]) and np.array_equal(ry, lab[10:15])
+    before, _ = net.gradients(x[:512], lab[:512])
+    after = net.train(pairs, steps=300, batch=256, lr=2e-3)
+    final, _ = net.gradients(x[:512], lab[:512])
+    assert final < 0.3 * before, (before, after, final)
+    net.close()
+    pairs.close()
+
+
+# ------------------------------------------------- the network in synthesis
+
+from resynthesizer_gb300 import workloads as W   # noqa: E402
+
+
+def test_dump_pairs_match_final_state():
+    wl = W.render(tile=48, out=64)
+    tgt, cor, kw = wl["target"], wl["corpus"], wl["params"]
+    fmt = R.format_indices(*wl["format"])
+    pairs = R.Pairs(100000)
+    stride = 7
+    r = R.engine(tgt, cor, fmt, R.params(**kw),
+                 opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1, dump=pairs, dumpStride=stride))
+    assert r.rc == 0
+    ys, xs = np.nonzero(tgt[..., 0] != 0)          # targets in raster order
+    pos = np.stack([xs, ys], 1)[::stride]
+    assert len(pairs) == len(pos)
+    x, lab = pairs.read()
+    colors = r.out[..., 1:1 + fmt.img_match_bpp]
+    valued = r.has_value.astype(bool)
+    src = r.source
+    for i in range(len(pos)):
+        tx, ty = pos[i]
+        assert lab[i, 0] == np.float32(src[ty, tx, 0] - tx) / 64 and lab[i, 1] == np.float32(src[ty, tx, 1] - ty) / 64
+        if i % 2:
+            # complete context: exactly the final image around the target
+            assert np.array_equal(x[i], N.context(colors, valued, None, tx, ty)), i
+        else:
+            # the context at the target's first visit: a subset of the final
+            # one with the same colours where it has values
+            full = N.bits_to_float(N.context(colors, valued, None, tx, ty))
+            part = N.bits_to_float(x[i])
+            h = part[..., 3] > 0
+            assert (full[..., 3][h] > 0).all() and np.array_equal(part[h], full[h])
+            assert not h[5, 5]             # the target itself had no value yet
+    pairs.close()
+
+
+def _heal_run(wl, net=None, proposals=0, trys=None):
+    tgt, cor = W.simple_to_pixmaps(wl["image"], wl["mask"])
+    kw = dict(wl["params"])
+    if trys is not None:
+        kw["maxProbeCount"] = trys
+    fmt = R.format_indices(3, 0, 0, 0, 0)
+    r = R.engine(tgt, cor, fmt, R.params(**kw),
+                 opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1, net=net, proposals=proposals))
+    assert r.rc == 0
+    sel = tgt[..., 0] != 0
+    ys, xs = np.nonzero(sel)
+    targets = np.stack([xs, ys], 1).astype(np.int32)
+    e, _ = R.patch_energy(R.params(**kw), fmt, r.out, cor, r.has_value, r.source, targets)
+    return r, e, tgt, cor, sel
+
+
+def test_wavefront_with_proposals_keeps_invariants(net):
+    wl = W.heal_small(size=96, hole=40, ctype=2, patch=30, trys=200)
+    r, e, tgt, cor, sel = _heal_run(wl, net=net, proposals=16)
+    r2, e2, *_ = _heal_run(wl, net=net, proposals=16)
+    assert (r.out == r2.out).all() and e == e2          # deterministic
+    assert (r.out[~sel] == tgt[~sel]).all()
+    src = r.source[sel]
+    assert (src[:, 0] >= 0).all() and r.has_value[sel].all()
+    assert (r.out[sel][:, 1:4] == cor[src[:, 1], src[:, 0], 1:4]).all()
+    assert r.stats["evals"] > 0
+    # only the network's candidates and the continuations: still a valid synthesis
+    r0, e0, *_ = _heal_run(wl, net=net, proposals=16, trys=0)
+    assert (r0.source[sel][:, 0] >= 0).all()
