@@ -184,3 +184,35 @@ def test_wavefront_with_proposals_keeps_invariants(net):
     # only the network's candidates and the continuations: still a valid synthesis
     r0, e0, *_ = _heal_run(wl, net=net, proposals=16, trys=0)
     assert (r0.source[sel][:, 0] >= 0).all()
+
+
+def test_trained_network_gain():
+    """Train on pairs dumped by plain runs, then synthesize a held-out image.
+    With no random probes the continuations alone cannot start a heal (no
+    context pixel has a source), so the network's proposals are the only new
+    candidates: the trained network must beat both no network and the
+    untrained one, and lower the loss on held-out pairs."""
+    pairs = R.Pairs(400000)
+    for i in range(1, 5):
+        wl = W.heal4096(index=i, size=192)
+        tgt, cor = W.simple_to_pixmaps(wl["image"], wl["mask"])
+        r = R.engine(tgt, cor, R.format_indices(3, 0, 0, 0, 0), R.params(**wl["params"]),
+                     opts=R.options(mode=R.MODE_WAVEFRONT, dump=pairs, dumpStride=1))
+        assert r.rc == 0
+    held = R.Pairs(100000)
+    wl0 = W.heal4096(index=0, size=192)
+    tgt, cor = W.simple_to_pixmaps(wl0["image"], wl0["mask"])
+    assert R.engine(tgt, cor, R.format_indices(3, 0, 0, 0, 0), R.params(**wl0["params"]),
+                    opts=R.options(mode=R.MODE_WAVEFRONT, dump=held, dumpStride=1)).rc == 0
+    hx, hy = held.read()
+    untrained = R.Net(seed=21)
+    trained = R.Net(seed=21)
+    trained.train(pairs, steps=600, batch=512, lr=1e-3)
+    assert trained.gradients(hx, hy)[0] < untrained.gradients(hx, hy)[0]
+    _, e_plain, *_ = _heal_run(wl0, trys=0)
+    _, e_untrained, *_ = _heal_run(wl0, net=untrained, proposals=16, trys=0)
+    _, e_trained, *_ = _heal_run(wl0, net=trained, proposals=16, trys=0)
+    assert e_trained < 0.5 * e_plain, (e_trained, e_plain)
+    assert e_trained < e_untrained, (e_trained, e_untrained)
+    for o in (pairs, held, untrained, trained):
+        o.close()
