@@ -234,6 +234,17 @@ int resynthPatchEnergy(const TImageSynthParameters *parameters, const TFormatInd
                        const Coordinates *targets, unsigned int targetCount,
                        unsigned long long *energy, unsigned int *perTarget);
 
+/* No counterpart in the reference.  Test entry of the two pass-0 patch
+ * builders of wavefront mode: for each target (a pixel without a value), the
+ * offsets (dx, dy) of its patch neighbours in patch order, self excluded, as
+ * prepare_neighbors (lib/synthesize.h:158-241) chooses them under the
+ * wavefront offset radius, found by walking the sorted offset list (useGrid
+ * 0) or from the cell grid of least visit stamps (useGrid 1).  hasValue is
+ * width x height bytes; offsets receives n x 63 Coordinates, counts n. */
+int resynthPatchNeighbours(const unsigned char *hasValue, unsigned int width, unsigned int height,
+                           unsigned int patchSize, const Coordinates *targets, unsigned int n, int useGrid,
+                           Coordinates *offsets, unsigned int *counts);
+
 /* No counterpart in the reference.  Frozen-state best fit, as
  * resynthFrozenBestFit, for callers that cannot let a library allocate device
  * memory -- a host application that reserves the GPU's memory up front and

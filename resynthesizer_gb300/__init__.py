@@ -136,6 +136,7 @@ def lib() -> C.CDLL:
         L.invert_bytemap.argtypes = [P(Map)]
         L.interleave_mask.argtypes = [P(Map), P(Map)]
         L.resynthTcGemm.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp]
+        L.resynthPatchNeighbours.argtypes = [vp, u, u, u, vp, u, C.c_int, vp, vp]
         L.resynthNetParamCount.restype = u
         L.resynthNetCreate.argtypes = [u]
         L.resynthNetCreate.restype = vp
@@ -468,3 +469,15 @@ class Pairs:
 def _check(rc, what):
     if rc:
         raise RuntimeError(f"{what} rc={rc}: {last_error()}")
+
+
+def patch_neighbours(has_value: np.ndarray, patch_size: int, targets: np.ndarray, use_grid: bool):
+    """resynthPatchNeighbours: per target, the (dx, dy) of its patch neighbours."""
+    hv = np.ascontiguousarray(has_value, np.uint8)
+    h, w = hv.shape
+    t = np.ascontiguousarray(targets, np.int32)
+    off = np.zeros((len(t), 63, 2), np.int32)
+    cnt = np.zeros(len(t), np.uint32)
+    _check(lib().resynthPatchNeighbours(_vp(hv), w, h, patch_size, _vp(t), len(t), int(use_grid), _vp(off), _vp(cnt)),
+           "resynthPatchNeighbours")
+    return [off[i, :cnt[i]] for i in range(len(t))]

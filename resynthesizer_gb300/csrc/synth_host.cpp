@@ -722,9 +722,9 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     CK(rs_vis_init(dp.pb.has, (int)(tw * th), vis, s));
     launches++;
     wa.pb.vis = vis;
-    // Stores go straight into the state unless the target wraps (tiling): then
-    // colour phases can meet across the seam, and results are staged.
-    wa.inPlace = (dp.pb.tileH || dp.pb.tileV) ? 0 : 1;
+    const bool tiled = dp.pb.tileH || dp.pb.tileV;
+    const int cellsW = ((int)tw + rs::kCell - 1) >> rs::kCellShift, cellsH = ((int)th + rs::kCell - 1) >> rs::kCellShift;
+    int* cellMin = tiled ? nullptr : ar.alloc<int>((size_t)cellsW * cellsH);
     int* batchStart = ar.alloc<int>((size_t)kMaxBands * k * k + 1);
     int* work = ar.alloc<int>(3 * (size_t)kMaxBands * k * k + 1 + ntargets);
     wa.targets = dPass;
@@ -771,6 +771,22 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       CK(rs_prep_batches(dTargets, (int)ntargets, (int)tw, (int)end, randomOrder ? 1 : 0, wa.seed ^ 0x5bd1e995u,
                          dBandEnds, dBandPhased, nb, k, work, batchStart, dPass, pass == 0 ? vis : nullptr, s));
       launches += 4;
+      // Pass 0: the least visit stamp per cell lets far-reaching patches skip
+      // the empty parts of the image (no wrapping: tiled targets walk the list).
+      // Pass-0 stores go straight into the state: no target of a batch reads
+      // another (visit stamps).  Later passes read every neighbour, and near
+      // the image border a patch reaches past the colour-phase spacing, so
+      // their results are staged and applied after each batch; so are those
+      // of wrapping (tiled) targets, whose phases can meet across the seam.
+      wa.inPlace = (tiled || pass > 0) ? 0 : 1;
+      wa.pb.cellMin = nullptr;
+      if (pass == 0 && cellMin) {
+        CK(rs_cell_min(vis, (int)tw, (int)th, cellMin, s));
+        launches++;
+        wa.pb.cellMin = cellMin;
+        wa.pb.cellsW = cellsW;
+        wa.pb.cellsH = cellsH;
+      }
       const int nbatches = nb * k * k;
       wa.pass = (unsigned)pass;
       wa.sparse = (pass == 0 && sparseOk) ? 1 : 0;
@@ -1296,6 +1312,65 @@ RS_EXPORT int resynthFrozenBestFit(const TImageSynthParameters* p, const TFormat
   return guarded("resynthFrozenBestFit", [&] {
     return score_host(false, p, f, target, tw, th, corpus, cw, ch, hasValue, sourceOf, targets, n, candStart, cands,
                       bestSum, bestPoint, patchCount, nullptr);
+  });
+}
+
+RS_EXPORT int resynthPatchNeighbours(const unsigned char* hasValue, unsigned int width, unsigned int height,
+                                     unsigned int patchSize, const Coordinates* targets, unsigned int n, int useGrid,
+                                     Coordinates* offsets, unsigned int* counts) {
+  if (!hasValue || !targets || !offsets || !counts || !width || !height)
+    return fail(RESYNTH_ERROR_ARGUMENT, "NULL argument");
+  if (patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+  return guarded("resynthPatchNeighbours", [&] {
+    Stream& st = thread_stream();
+    cudaStream_t s = st.s;
+    Arena ar(s);
+    unsigned long long h2d = 0;
+    const int w = (int)width, h = (int)height;
+    const size_t npx = (size_t)w * h;
+    const long long maxD2 = wave_radius2(w, h);
+    const auto offsHeld = cached_offsets(w, h, maxD2);
+    const std::vector<int2>& offs = *offsHeld;
+    rs::Problem pb{};
+    pb.tw = pb.cw = w;
+    pb.th = pb.ch = h;
+    pb.nc = 1;
+    pb.has = ar.upload(hasValue, npx, h2d);
+    int* vis = ar.alloc<int>(npx);
+    CK(rs_vis_init(pb.has, (int)npx, vis, s));
+    pb.vis = vis;
+    pb.tpx = ar.alloc<uint32_t>(npx);
+    CK(cudaMemsetAsync(pb.tpx, 0, npx * sizeof(uint32_t), s));
+    pb.src = ar.alloc<int2>(npx);
+    CK(cudaMemsetAsync(pb.src, 0xFF, npx * sizeof(int2), s));
+    pb.offs = ar.upload(offs.data(), offs.size(), h2d);
+    pb.noffs = (int)offs.size();
+    pb.patchLimit = (int)std::max(patchSize, 2u);
+    pb.boxW = w;
+    pb.boxH = h;
+    pb.maxD2 = maxD2;
+    pb.cellsW = (w + rs::kCell - 1) >> rs::kCellShift;
+    pb.cellsH = (h + rs::kCell - 1) >> rs::kCellShift;
+    int* cellMin = ar.alloc<int>((size_t)pb.cellsW * pb.cellsH);
+    CK(rs_cell_min(vis, w, h, cellMin, s));
+    pb.cellMin = cellMin;
+    const int2* dT = ar.upload(reinterpret_cast<const int2*>(targets), n, h2d);
+    int* dOff = ar.alloc<int>((size_t)n * rs::kMaxNeighbors);
+    int* dCnt = ar.alloc<int>(n);
+    // valued = hasValue: stamp -1 < 0
+    if (n) CK(rs_launch_patches(pb, dT, (int)n, 0, useGrid ? 1 : 0, dOff, dCnt, s));
+    std::vector<int> hOff((size_t)n * rs::kMaxNeighbors), hCnt(n);
+    CK(cudaMemcpyAsync(hOff.data(), dOff, hOff.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hCnt.data(), dCnt, hCnt.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (unsigned t = 0; t < n; t++) {
+      counts[t] = (unsigned)hCnt[t];
+      for (int i = 0; i < hCnt[t]; i++) {
+        const int o = hOff[(size_t)t * rs::kMaxNeighbors + i];
+        offsets[(size_t)t * (rs::kMaxNeighbors - 1) + i] = Coordinates{(int)(int16_t)(o & 0xffff), o >> 16};
+      }
+    }
+    return 0;
   });
 }
 

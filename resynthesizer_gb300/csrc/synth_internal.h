@@ -42,7 +42,13 @@ struct Problem {
   uint32_t clipCost;          // 65535 * nc + mapTable[0] * nm
   const uint32_t* ctab;       // colour metric table (512 entries, widened to 32 bits)
   const uint32_t* mtab;       // map metric table (512)
+  const int* cellMin;         // wavefront pass 0: least visit stamp of each kCell x kCell cell, or null
+  int cellsW, cellsH;
 };
+
+// Side of the cells of Problem::cellMin (a power of two).
+constexpr int kCellShift = 3;
+constexpr int kCell = 1 << kCellShift;
 
 // Device counters accumulated by the synthesis kernels.
 struct Counters {
@@ -129,6 +135,9 @@ cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, siz
 cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow, cudaStream_t s);
 cudaError_t rs_vis_init(const uint8_t* has, int npx, int* vis, cudaStream_t s);
 cudaError_t rs_vis_to_has(const int* vis, int npx, uint8_t* has, cudaStream_t s);
+cudaError_t rs_cell_min(const int* vis, int tw, int th, int* cellMin, cudaStream_t s);
+cudaError_t rs_launch_patches(const rs::Problem& pb, const int2* targets, int n, int visCur, int useGrid, int* outOff,
+                              int* outCount, cudaStream_t s);
 }
 
 // Proposal network (proposal_net.cu).

@@ -95,16 +95,19 @@ __device__ __forceinline__ void load_nb(const Problem& pb, Patch& P, int slot, i
 // prepare_neighbors for one target with one warp: the target itself first,
 // then the nearest sorted offsets whose point lies in (or wraps into) the
 // target image and has a value, until the patch limit.  Returns the count.
-__device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int lane, int visCur = 0) {
+// At most maxOffsets entries of the offset list are examined.
+__device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int lane, int visCur = 0,
+                                int maxOffsets = INT_MAX) {
   if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
   int count = 1;
   const int limit = pb.patchLimit;
-  for (int base = 1; base < pb.noffs && count < limit; base += 32) {
+  const int noffs = min(pb.noffs, maxOffsets);
+  for (int base = 1; base < noffs && count < limit; base += 32) {
     const int j = base + lane;
     bool ok = false;
     int qi = 0;
     int2 o = make_int2(0, 0);
-    if (j < pb.noffs) {
+    if (j < noffs) {
       o = __ldg(&pb.offs[j]);
       int qx = px + o.x, qy = py + o.y;
       if (wrap_or_clip(pb, qx, qy)) {
@@ -175,6 +178,125 @@ __device__ int build_patch_sparse(const Problem& pb, int px, int py, Patch& P, u
   __syncwarp();
   return 1 + cnt;
 }
+
+// Inserts one key per lane into the warp's ascending list best[0 .. cnt)
+// holding the lim smallest keys seen; thr = the lim-th key once full.
+__device__ __forceinline__ void topk_insert(unsigned long long key, unsigned long long* best, int& cnt,
+                                            unsigned long long& thr, int lim, int lane) {
+  unsigned m = __ballot_sync(kFull, key < thr);
+  while (m) {
+    const int srcLane = __ffs(m) - 1;
+    m &= m - 1;
+    const unsigned long long k = __shfl_sync(kFull, key, srcLane);
+    if (k >= thr) continue;
+    const unsigned long long e0 = lane < cnt ? best[lane] : ~0ull;
+    const unsigned long long e1 = lane + 32 < cnt ? best[lane + 32] : ~0ull;
+    const int pos = __popc(__ballot_sync(kFull, e0 < k)) + __popc(__ballot_sync(kFull, e1 < k));
+    __syncwarp();
+    if (lane >= pos && lane < cnt && lane + 1 < lim) best[lane + 1] = e0;
+    if (lane + 32 >= pos && lane + 32 < cnt && lane + 33 < lim) best[lane + 33] = e1;
+    __syncwarp();
+    if (lane == 0) best[pos] = k;
+    __syncwarp();
+    cnt = min(cnt + 1, lim);
+    thr = cnt == lim ? best[lim - 1] : ~0ull;
+  }
+}
+
+// The pass-0 patch of a target from the cell grid (no wrapping): the
+// nearest pixels with a value in sorted-offset order (ascending dx^2 + dy^2,
+// ties by descending position in the offset box), found by visiting the
+// kCell x kCell cells in rings of growing distance, skipping cells where no
+// pixel has a value yet (least visit stamp) or that lie beyond the current
+// patch's farthest neighbour.  Same neighbours as walking the offset list;
+// cheap when the nearest values are far away (deep inside a hole).
+__device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, unsigned long long* best, int lane,
+                                int visCur) {
+  if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
+  const int lim = pb.patchLimit - 1;
+  const int bw = pb.boxW, bh = pb.boxH;
+  const unsigned W2 = 2u * bw - 1u;
+  int cnt = 0;
+  unsigned long long thr = ~0ull;
+  const int cx = px >> kCellShift, cy = py >> kCellShift;
+  const int rmax = max(max(cx, pb.cellsW - 1 - cx), max(cy, pb.cellsH - 1 - cy));
+  for (int R = 0; R <= rmax; R++) {
+    if (R >= 1) {
+      // every pixel of ring R is at least (R - 1) * kCell + 1 away on one axis
+      const long long dmin = (long long)(R - 1) * kCell + 1;
+      if (dmin * dmin > pb.maxD2 || (dmin >= bw && dmin >= bh)) break;
+      if (cnt == lim && (unsigned long long)(dmin * dmin) > (thr >> 32)) break;
+    }
+    const int ncell = R == 0 ? 1 : 8 * R;
+    for (int c0 = 0; c0 < ncell; c0 += 32) {
+      const int ci = c0 + lane;
+      bool want = false;
+      int qcx = cx, qcy = cy;
+      if (ci < ncell) {
+        if (R > 0) {
+          const int side = ci / (2 * R), o = ci - side * 2 * R;
+          if (side == 0) {
+            qcx = cx - R + o;
+            qcy = cy - R;
+          } else if (side == 1) {
+            qcx = cx + R;
+            qcy = cy - R + o;
+          } else if (side == 2) {
+            qcx = cx + R - o;
+            qcy = cy + R;
+          } else {
+            qcx = cx - R;
+            qcy = cy + R - o;
+          }
+        }
+        if (qcx >= 0 && qcy >= 0 && qcx < pb.cellsW && qcy < pb.cellsH &&
+            pb.cellMin[qcy * pb.cellsW + qcx] < visCur) {
+          const int x0 = qcx << kCellShift, y0 = qcy << kCellShift;
+          const int ddx = max(0, max(x0 - px, px - (x0 + kCell - 1)));
+          const int ddy = max(0, max(y0 - py, py - (y0 + kCell - 1)));
+          const long long d2 = (long long)ddx * ddx + (long long)ddy * ddy;
+          want = d2 <= pb.maxD2 && ddx < bw && ddy < bh && (cnt < lim || (unsigned long long)d2 <= (thr >> 32));
+        }
+      }
+      unsigned wm = __ballot_sync(kFull, want);
+      while (wm) {
+        const int src = __ffs(wm) - 1;
+        wm &= wm - 1;
+        const int scx = __shfl_sync(kFull, qcx, src), scy = __shfl_sync(kFull, qcy, src);
+        // lane: row lane / 4 of the cell, 2 columns from (lane & 3) * 2
+        static_assert(kCell == 8, "one 8 x 8 cell per warp pass");
+        const int qy = (scy << kCellShift) + (lane >> 2);
+        const int qx0 = (scx << kCellShift) + (lane & 3) * 2;
+        unsigned long long keys[2];
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+          const int qx = qx0 + j, dx = qx - px, dy = qy - py;
+          unsigned long long key = ~0ull;
+          if (qx < pb.tw && qy < pb.th && dx > -bw && dx < bw && dy > -bh && dy < bh) {
+            const long long d2 = (long long)dx * dx + (long long)dy * dy;
+            if (d2 <= pb.maxD2 && pb.vis[qy * pb.tw + qx] < visCur) {
+              const unsigned idx = (unsigned)(dy + bh - 1) * W2 + (unsigned)(dx + bw - 1);
+              key = ((unsigned long long)d2 << 32) | (0xFFFFFFFFu - idx);
+            }
+          }
+          keys[j] = key;
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) topk_insert(keys[j], best, cnt, thr, lim, lane);
+      }
+    }
+  }
+  for (int i = lane; i < cnt; i += 32) {
+    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
+    const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
+    load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
+  }
+  __syncwarp();
+  return 1 + cnt;
+}
+
+// Offsets walked before a pass-0 patch falls back to the cell grid.
+constexpr int kScanCap = 512;
 
 // One neighbour term of computeBestFit for candidate (cx, cy): the clip/mask
 // penalty, or the colour terms (skipped for the target itself) plus the map
@@ -719,8 +841,14 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
     const int2 pos = a.targets[t];
     const int pi = pos.y * pb.tw + pos.x;
     if (tw == 0) {
-      const int n = sparse ? build_patch_sparse(pb, pos.x, pos.y, P, topk, a.targets, b0, lane)
-                           : build_patch_warp(pb, pos.x, pos.y, P, lane, a.visCur);
+      int n;
+      if (sparse) {
+        n = build_patch_sparse(pb, pos.x, pos.y, P, topk, a.targets, b0, lane);
+      } else {
+        n = build_patch_warp(pb, pos.x, pos.y, P, lane, a.visCur, pb.cellMin ? kScanCap : INT_MAX);
+        if (pb.cellMin && n < pb.patchLimit && kScanCap < pb.noffs)
+          n = build_patch_grid(pb, pos.x, pos.y, P, topk, lane, a.visCur);
+      }
       // linear offsets into the padded corpus; the fast path needs all within kPad
       int far = 0;
       for (int i = lane; i < n; i += 32) {
@@ -953,6 +1081,30 @@ extern "C" cudaError_t rs_launch_frozen(const ScoreArgs& a, cudaStream_t s) {
 
 extern "C" cudaError_t rs_launch_energy(const ScoreArgs& a, cudaStream_t s) {
   RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (k_energy<NC, MAP><<<grid_for(a.n, 8, sm_count() * 8), 256, 0, s>>>(a)));
+  return cudaGetLastError();
+}
+
+// The pass-0 patch of each listed target (pixels with vis < visCur have a
+// value) by the offset-list walk or by the cell grid: neighbour offsets in
+// patch order, self excluded.  Checks that both builders agree.
+__global__ void __launch_bounds__(256) k_patches(Problem pb, const int2* targets, int n, int visCur, int useGrid,
+                                                 int* outOff, int* outCount) {
+  __shared__ Patch sp[8];
+  __shared__ unsigned long long sk[8][kMaxNeighbors];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int t = blockIdx.x * 8 + w; t < n; t += gridDim.x * 8) {
+    const int2 pos = targets[t];
+    const int cnt = useGrid ? build_patch_grid(pb, pos.x, pos.y, sp[w], sk[w], lane, visCur)
+                            : build_patch_warp(pb, pos.x, pos.y, sp[w], lane, visCur);
+    for (int i = 1 + lane; i < cnt; i += 32) outOff[(size_t)t * kMaxNeighbors + i - 1] = sp[w].off[i];
+    if (lane == 0) outCount[t] = cnt - 1;
+    __syncwarp();
+  }
+}
+
+extern "C" cudaError_t rs_launch_patches(const Problem& pb, const int2* targets, int n, int visCur, int useGrid,
+                                         int* outOff, int* outCount, cudaStream_t s) {
+  k_patches<<<grid_for(n, 8, sm_count() * 8), 256, 0, s>>>(pb, targets, n, visCur, useGrid, outOff, outCount);
   return cudaGetLastError();
 }
 

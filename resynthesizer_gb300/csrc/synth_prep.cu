@@ -272,8 +272,30 @@ __global__ void k_vis_to_has(const int* vis, int npx, uint8_t* has) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x)
     has[i] = vis[i] != 0x7fffffff ? 1 : 0;
 }
+// Least visit stamp of each kCell x kCell cell: a pixel of the cell can have
+// a value during batch b only if the cell's minimum is below b.
+__global__ void k_cell_min(const int* vis, int tw, int th, int* cellMin) {
+  const int cw = (tw + kCell - 1) >> kCellShift, ch = (th + kCell - 1) >> kCellShift;
+  const int lane = threadIdx.x & 31;
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < cw * ch; c += (gridDim.x * blockDim.x) >> 5) {
+    const int x0 = (c % cw) << kCellShift, y0 = (c / cw) << kCellShift;
+    int m = 0x7fffffff;
+    for (int i = lane; i < kCell * kCell; i += 32) {
+      const int x = x0 + (i & (kCell - 1)), y = y0 + (i >> kCellShift);
+      if (x < tw && y < th) m = min(m, vis[y * tw + x]);
+    }
+    for (int o = 16; o; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) cellMin[c] = m;
+  }
+}
 }  // namespace
 }  // namespace rs
+
+extern "C" cudaError_t rs_cell_min(const int* vis, int tw, int th, int* cellMin, cudaStream_t s) {
+  const int cells = ((tw + kCell - 1) >> kCellShift) * ((th + kCell - 1) >> kCellShift);
+  k_cell_min<<<std::min(blocks_for(cells * 32, 256), 4096), 256, 0, s>>>(vis, tw, th, cellMin);
+  return cudaGetLastError();
+}
 
 extern "C" cudaError_t rs_vis_init(const uint8_t* has, int npx, int* vis, cudaStream_t s) {
   k_vis_init<<<std::min(blocks_for(npx, 256), 2048), 256, 0, s>>>(has, npx, vis);

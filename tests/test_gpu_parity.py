@@ -215,12 +215,35 @@ def test_wavefront_invariants_and_energy(oracle, case):
     assert e_gpu <= 1.25 * e_ref, (e_gpu, e_ref)
 
 
-def test_wavefront_deterministic():
-    wl = W.render(tile=32, out=80)
+@pytest.mark.parametrize("out", [80, 300])
+def test_wavefront_deterministic(out):
+    # Near the image border a refinement-pass patch reaches past the colour
+    # phase spacing: the result must still not depend on the order in which
+    # the targets of one batch run.
+    wl = W.render(tile=32, out=out)
     fmt = R.format_indices(*wl["format"])
-    a = R.engine(wl["target"], wl["corpus"], fmt, R.params(**wl["params"]), opts=R.options(mode=R.MODE_WAVEFRONT))
-    b = R.engine(wl["target"], wl["corpus"], fmt, R.params(**wl["params"]), opts=R.options(mode=R.MODE_WAVEFRONT))
-    assert a.rc == b.rc == 0 and (a.out == b.out).all()
+    runs = [R.engine(wl["target"], wl["corpus"], fmt, R.params(**wl["params"]),
+                     opts=R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=w)) for w in (16, 16, 8, 4)]
+    assert all(r.rc == 0 for r in runs)
+    assert all((r.out == runs[0].out).all() for r in runs[1:])
+
+
+@pytest.mark.parametrize("density", [0.0005, 0.01, 0.2])
+def test_cell_grid_patches_equal_offset_walk(density):
+    # the pass-0 patch builder for far-reaching patches (cell grid) against
+    # the offset-list walk, over sparse value maps and targets deep in holes
+    rng = np.random.default_rng(int(density * 1e4))
+    h, w = 300, 420
+    hv = (rng.random((h, w)) < density).astype(np.uint8)
+    hv[100:260, 50:300] = 0                      # a large hole
+    ys, xs = np.nonzero(hv == 0)
+    pick = rng.choice(len(xs), 300, replace=False)
+    targets = np.stack([xs[pick], ys[pick]], 1)
+    for p in (9, 16, 30, 64):
+        a = R.patch_neighbours(hv, p, targets, use_grid=False)
+        b = R.patch_neighbours(hv, p, targets, use_grid=True)
+        for i in range(len(targets)):
+            assert np.array_equal(a[i], b[i]), (p, i)
 
 
 def test_batch_matches_single_calls(oracle):
