@@ -124,61 +124,6 @@ __device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int
   return count;
 }
 
-// The same patch when the valued pixels are exactly list[0 .. V) and nothing
-// wraps: the nearest valued pixels in sorted-offset order (ascending
-// dx^2 + dy^2, ties by descending position in the offset box -- the order of
-// the offset list), selected by a warp-wide insertion into a sorted top list
-// instead of walking the offset list.  Much cheaper while V is small.
-__device__ int build_patch_sparse(const Problem& pb, int px, int py, Patch& P, unsigned long long* best,
-                                  const int2* list, int V, int lane) {
-  if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
-  const int lim = pb.patchLimit - 1;
-  const int bw = pb.boxW, bh = pb.boxH;
-  const unsigned W2 = 2u * bw - 1u;
-  int cnt = 0;
-  unsigned long long thr = ~0ull;
-  for (int base = 0; base < V; base += 32) {
-    const int j = base + lane;
-    unsigned long long key = ~0ull;
-    if (j < V) {
-      const int2 q = list[j];
-      const int dx = q.x - px, dy = q.y - py;
-      if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
-        const long long d2 = (long long)dx * dx + (long long)dy * dy;
-        if (d2 <= pb.maxD2) {
-          const unsigned idx = (unsigned)(dy + bh - 1) * W2 + (unsigned)(dx + bw - 1);
-          key = ((unsigned long long)d2 << 32) | (0xFFFFFFFFu - idx);
-        }
-      }
-    }
-    unsigned m = __ballot_sync(kFull, key < thr);
-    while (m) {
-      const int srcLane = __ffs(m) - 1;
-      m &= m - 1;
-      const unsigned long long k = __shfl_sync(kFull, key, srcLane);
-      if (k >= thr) continue;
-      const unsigned long long e0 = lane < cnt ? best[lane] : ~0ull;
-      const unsigned long long e1 = lane + 32 < cnt ? best[lane + 32] : ~0ull;
-      const int pos = __popc(__ballot_sync(kFull, e0 < k)) + __popc(__ballot_sync(kFull, e1 < k));
-      __syncwarp();
-      if (lane >= pos && lane < cnt && lane + 1 < lim) best[lane + 1] = e0;
-      if (lane + 32 >= pos && lane + 32 < cnt && lane + 33 < lim) best[lane + 33] = e1;
-      __syncwarp();
-      if (lane == 0) best[pos] = k;
-      __syncwarp();
-      cnt = min(cnt + 1, lim);
-      thr = cnt == lim ? best[lim - 1] : ~0ull;
-    }
-  }
-  for (int i = lane; i < cnt; i += 32) {
-    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
-    const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
-    load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
-  }
-  __syncwarp();
-  return 1 + cnt;
-}
-
 // Inserts one key per lane into the warp's ascending list best[0 .. cnt)
 // holding the lim smallest keys seen; thr = the lim-th key once full.
 __device__ __forceinline__ void topk_insert(unsigned long long key, unsigned long long* best, int& cnt,
@@ -203,21 +148,75 @@ __device__ __forceinline__ void topk_insert(unsigned long long key, unsigned lon
   }
 }
 
-// The pass-0 patch of a target from the cell grid (no wrapping): the
-// nearest pixels with a value in sorted-offset order (ascending dx^2 + dy^2,
-// ties by descending position in the offset box), found by visiting the
-// kCell x kCell cells in rings of growing distance, skipping cells where no
-// pixel has a value yet (least visit stamp) or that lie beyond the current
-// patch's farthest neighbour.  Same neighbours as walking the offset list;
-// cheap when the nearest values are far away (deep inside a hole).
-__device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, unsigned long long* best, int lane,
-                                int visCur) {
-  if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
-  const int lim = pb.patchLimit - 1;
+// Sort key of neighbour offset (dx, dy): the sorted offset list's order,
+// ascending dx^2 + dy^2 with ties by descending position in the offset box.
+__device__ __forceinline__ unsigned long long offset_key(const Problem& pb, int dx, int dy) {
+  const unsigned W2 = 2u * pb.boxW - 1u;
+  const unsigned idx = (unsigned)(dy + pb.boxH - 1) * W2 + (unsigned)(dx + pb.boxW - 1);
+  return ((unsigned long long)((long long)dx * dx + (long long)dy * dy) << 32) | (0xFFFFFFFFu - idx);
+}
+
+// The patch from a finished key list: self, then the listed neighbours.
+__device__ int patch_from_keys(const Problem& pb, int px, int py, Patch& P, const unsigned long long* best, int cnt,
+                               int lane) {
   const int bw = pb.boxW, bh = pb.boxH;
   const unsigned W2 = 2u * bw - 1u;
-  int cnt = 0;
-  unsigned long long thr = ~0ull;
+  if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
+  for (int i = lane; i < cnt; i += 32) {
+    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
+    const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
+    load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
+  }
+  __syncwarp();
+  return 1 + cnt;
+}
+
+// Merges other key lists into best (a list of the lim smallest keys).
+__device__ void merge_keys(unsigned long long* best, int& cnt, unsigned long long& thr, int lim,
+                           const unsigned long long* other, int ocnt, int lane) {
+  for (int base = 0; base < ocnt; base += 32) {
+    const unsigned long long k = base + lane < ocnt ? other[base + lane] : ~0ull;
+    topk_insert(k, best, cnt, thr, lim, lane);
+  }
+}
+
+// Patch neighbours when the valued pixels are exactly list[0 .. V) and nothing
+// wraps: the lim nearest in sorted-offset order, by a warp-wide insertion into
+// a sorted key list instead of walking the offset list.  Part `part` of
+// `parts` warps takes every parts-th run of 32 list entries; merging the
+// parts' lists gives the whole list's lim smallest keys.
+__device__ void sparse_keys(const Problem& pb, int px, int py, unsigned long long* best, int& cnt,
+                            unsigned long long& thr, const int2* list, int V, int lane, int part, int parts) {
+  const int lim = pb.patchLimit - 1;
+  const int bw = pb.boxW, bh = pb.boxH;
+  for (int base = part * 32; base < V; base += 32 * parts) {
+    const int j = base + lane;
+    unsigned long long key = ~0ull;
+    if (j < V) {
+      const int2 q = list[j];
+      const int dx = q.x - px, dy = q.y - py;
+      if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
+        const long long d2 = (long long)dx * dx + (long long)dy * dy;
+        if (d2 <= pb.maxD2) key = offset_key(pb, dx, dy);
+      }
+    }
+    topk_insert(key, best, cnt, thr, lim, lane);
+  }
+}
+
+// Patch neighbours of a pass-0 target from the cell grid (no wrapping): the
+// pixels with a value in sorted-offset order, found by visiting the kCell x
+// kCell cells in rings of growing distance, skipping cells where no pixel
+// has a value yet (least visit stamp) or that lie beyond the list's current
+// last entry.  Same neighbours as walking the offset list; cheap when the
+// nearest values are far away (deep inside a hole).  Part `part` of `parts`
+// warps owns the cells whose ring index is congruent to it; each part stops
+// on its own bound, and merging the parts' lists gives the lim smallest keys
+// (a key among the lim smallest overall is among the lim smallest of its part).
+__device__ void grid_keys(const Problem& pb, int px, int py, unsigned long long* best, int& cnt,
+                          unsigned long long& thr, int lane, int visCur, int part, int parts) {
+  const int lim = pb.patchLimit - 1;
+  const int bw = pb.boxW, bh = pb.boxH;
   const int cx = px >> kCellShift, cy = py >> kCellShift;
   const int rmax = max(max(cx, pb.cellsW - 1 - cx), max(cy, pb.cellsH - 1 - cy));
   for (int R = 0; R <= rmax; R++) {
@@ -228,11 +227,12 @@ __device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, uns
       if (cnt == lim && (unsigned long long)(dmin * dmin) > (thr >> 32)) break;
     }
     const int ncell = R == 0 ? 1 : 8 * R;
-    for (int c0 = 0; c0 < ncell; c0 += 32) {
-      const int ci = c0 + lane;
+    const int mine = ncell > part ? (ncell - part + parts - 1) / parts : 0;   // cells part, part + parts, ...
+    for (int c0 = 0; c0 < mine; c0 += 32) {
+      const int ci = (c0 + lane) * parts + part;
       bool want = false;
       int qcx = cx, qcy = cy;
-      if (ci < ncell) {
+      if (c0 + lane < mine) {
         if (R > 0) {
           const int side = ci / (2 * R), o = ci - side * 2 * R;
           if (side == 0) {
@@ -267,32 +267,28 @@ __device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, uns
         static_assert(kCell == 8, "one 8 x 8 cell per warp pass");
         const int qy = (scy << kCellShift) + (lane >> 2);
         const int qx0 = (scx << kCellShift) + (lane & 3) * 2;
-        unsigned long long keys[2];
 #pragma unroll
         for (int j = 0; j < 2; j++) {
           const int qx = qx0 + j, dx = qx - px, dy = qy - py;
           unsigned long long key = ~0ull;
           if (qx < pb.tw && qy < pb.th && dx > -bw && dx < bw && dy > -bh && dy < bh) {
             const long long d2 = (long long)dx * dx + (long long)dy * dy;
-            if (d2 <= pb.maxD2 && pb.vis[qy * pb.tw + qx] < visCur) {
-              const unsigned idx = (unsigned)(dy + bh - 1) * W2 + (unsigned)(dx + bw - 1);
-              key = ((unsigned long long)d2 << 32) | (0xFFFFFFFFu - idx);
-            }
+            if (d2 <= pb.maxD2 && pb.vis[qy * pb.tw + qx] < visCur) key = offset_key(pb, dx, dy);
           }
-          keys[j] = key;
+          topk_insert(key, best, cnt, thr, lim, lane);
         }
-#pragma unroll
-        for (int j = 0; j < 2; j++) topk_insert(keys[j], best, cnt, thr, lim, lane);
       }
     }
   }
-  for (int i = lane; i < cnt; i += 32) {
-    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
-    const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
-    load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
-  }
-  __syncwarp();
-  return 1 + cnt;
+}
+
+// One warp: the whole grid search.
+__device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, unsigned long long* best, int lane,
+                                int visCur) {
+  int cnt = 0;
+  unsigned long long thr = ~0ull;
+  grid_keys(pb, px, py, best, cnt, thr, lane, visCur, 0, 1);
+  return patch_from_keys(pb, px, py, P, best, cnt, lane);
 }
 
 // Offsets walked before a pass-0 patch falls back to the cell grid.
@@ -826,7 +822,7 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   unsigned long long* topk = reinterpret_cast<unsigned long long*>(wbase + sizeof(Patch));
   int2* prop = reinterpret_cast<int2*>(topk);
   __shared__ unsigned long long s_key[16];
-  __shared__ int s_n[16], s_np[16], s_fast[16];
+  __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16];
   __shared__ unsigned s_better;
   if (threadIdx.x == 0) s_better = 0;
   __syncthreads();
@@ -840,15 +836,33 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
     const int t = b0 + slot;
     const int2 pos = a.targets[t];
     const int pi = pos.y * pb.tw + pos.x;
-    if (tw == 0) {
-      int n;
-      if (sparse) {
-        n = build_patch_sparse(pb, pos.x, pos.y, P, topk, a.targets, b0, lane);
-      } else {
-        n = build_patch_warp(pb, pos.x, pos.y, P, lane, a.visCur, pb.cellMin ? kScanCap : INT_MAX);
-        if (pb.cellMin && n < pb.patchLimit && kScanCap < pb.noffs)
-          n = build_patch_grid(pb, pos.x, pos.y, P, topk, lane, a.visCur);
+    // The patch.  While the valued pixels are a short list, every warp of the
+    // team collects the nearest keys of its share of the list and the lead
+    // merges them; otherwise the lead walks the offset list, falling back to
+    // the cell grid when the nearest values lie beyond the walk's reach.
+    int nPatch = 0;
+    if (sparse) {
+      unsigned long long* mine = reinterpret_cast<unsigned long long*>(p + warp * WaveSmem::kPerWarp + sizeof(Patch));
+      int cnt = 0;
+      unsigned long long thr = ~0ull;
+      sparse_keys(pb, pos.x, pos.y, mine, cnt, thr, a.targets, b0, lane, tw, G);
+      if (G > 1) {
+        if (lane == 0) s_gather[warp] = cnt;
+        team_sync();
+        if (tw == 0)
+          for (int w = 1; w < G; w++)
+            merge_keys(mine, cnt, thr, pb.patchLimit - 1,
+                       reinterpret_cast<const unsigned long long*>(p + (lead + w) * WaveSmem::kPerWarp + sizeof(Patch)),
+                       s_gather[lead + w], lane);
       }
+      if (tw == 0) nPatch = patch_from_keys(pb, pos.x, pos.y, P, mine, cnt, lane);
+    } else if (tw == 0) {
+      nPatch = build_patch_warp(pb, pos.x, pos.y, P, lane, a.visCur, pb.cellMin ? kScanCap : INT_MAX);
+      if (pb.cellMin && nPatch < pb.patchLimit && kScanCap < pb.noffs)
+        nPatch = build_patch_grid(pb, pos.x, pos.y, P, topk, lane, a.visCur);
+    }
+    if (tw == 0) {
+      const int n = nPatch;
       // linear offsets into the padded corpus; the fast path needs all within kPad
       int far = 0;
       for (int i = lane; i < n; i += 32) {
