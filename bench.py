@@ -259,6 +259,70 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(args):
+    """Learned proposals against the plain search on the large heal (seeded
+    value noise, union of 40 ellipses covering ~10 % of the image): pairs are
+    dumped by plain wavefront runs over `--train-images` images (seeds 1..N),
+    the network trains on the GPU with the tensor-core kernels, then a
+    held-out image (seed 0) is synthesized with and without the network's 16
+    proposals at several probe counts.  Energy = sum of the full-patch metric
+    over the targets at their final sources."""
+    import numpy as np
+
+    import resynthesizer_gb300 as R
+    from resynthesizer_gb300 import workloads as W
+    size = args.learned_size
+    fmt = R.format_indices(3, 0, 0, 0, 0)
+
+    def run(wl, trys, net=None, dump=None, stride=16, state=True):
+        tgt, cor = W.simple_to_pixmaps(wl["image"], wl["mask"])
+        kw = dict(wl["params"])
+        kw["maxProbeCount"] = trys
+        o = R.options(mode=R.MODE_WAVEFRONT, recordState=1 if state else 0, net=net, proposals=16 if net else 0,
+                      dump=dump, dumpStride=stride)
+        r = R.engine(tgt, cor, fmt, R.params(**kw), opts=o)
+        assert r.rc == 0, R.last_error()
+        e = None
+        if state:
+            ys, xs = np.nonzero(tgt[..., 0] != 0)
+            t = np.stack([xs, ys], 1).astype(np.int32)
+            e, _ = R.patch_energy(R.params(**kw), fmt, r.out, cor, r.has_value, r.source, t)
+        return r, e
+
+    t0 = time.perf_counter()
+    pairs = R.Pairs(args.train_pairs)
+    per_image = max(1, args.train_pairs // args.train_images)
+    for i in range(1, args.train_images + 1):
+        wl = W.heal4096(index=i, size=size)
+        run(wl, 200, dump=pairs, stride=max(1, wl["target_px"] // per_image), state=False)
+    dump_s = time.perf_counter() - t0
+    net = R.Net(seed=1)
+    t0 = time.perf_counter()
+    loss = net.train(pairs, steps=args.train_steps, batch=512, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    wl = W.heal4096(index=0, size=size)
+    rows = []
+    for trys, use in [(200, False), (64, False), (16, False), (200, True), (64, True), (16, True), (0, True)]:
+        ms = []
+        for _ in range(3):
+            r, e = run(wl, trys, net=net if use else None)
+            ms.append(r.stats["deviceMs"])
+        rows.append({"search": ("learned+" if use else "plain ") + f"trys={trys}", "energy": e,
+                     "ms": min(ms), "px_per_s": wl["target_px"] / (min(ms) / 1000.0), "evals": r.stats["evals"],
+                     "passes": r.stats["passes"]})
+    base = rows[0]["energy"]
+    for row in rows:
+        row["energy_vs_plain200"] = row["energy"] / base
+    # the fastest learned search whose energy is at most the plain search's
+    ok = [row for row in rows if row["search"].startswith("learned") and row["energy"] <= base]
+    best = max(ok, key=lambda r: r["px_per_s"]) if ok else None
+    line = {"learned": f"heal{size}", "target_px": wl["target_px"], "train_images": args.train_images,
+            "train_pairs": len(pairs), "dump_s": dump_s, "train_steps": args.train_steps, "train_s": train_s,
+            "train_loss": loss, "rows": rows,
+            "learned_vs_plain_px_per_s_at_equal_energy": (best["px_per_s"] / rows[0]["px_per_s"]) if best else None}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference_arm(args):
     world, rank, _ = dist_setup()
     if rank != 0:
@@ -297,6 +361,11 @@ def main():
     ap.add_argument("--quality", action="store_true", help="energy against the CPU engine instead of speed")
     ap.add_argument("--quality-runs", type=int, default=3)
     ap.add_argument("--concurrency", type=int, default=8, help="host workers for batch workloads")
+    ap.add_argument("--learned", action="store_true", help="learned proposals against the plain search")
+    ap.add_argument("--learned-size", type=int, default=4096)
+    ap.add_argument("--train-images", type=int, default=64)
+    ap.add_argument("--train-pairs", type=int, default=2000000)
+    ap.add_argument("--train-steps", type=int, default=4000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -305,6 +374,10 @@ def main():
         from resynthesizer_gb300 import build as B
         B.build()
         return run_quality(args)
+    if args.learned:
+        from resynthesizer_gb300 import build as B
+        B.build()
+        return run_learned(args)
     if args.workload.startswith("batch"):
         from resynthesizer_gb300 import build as B
         B.build()

@@ -122,21 +122,39 @@ __device__ __forceinline__ uint32_t bf2(float lo, float hi) {
 // Channels 0-7 of one context pixel: colour 0-2 (grey repeated) as v/255 -
 // 0.5 where the pixel has a value, has-value, map 0 as m/255 - 0.5.  Pixels
 // outside the target image are zero.  Channels 8-15 are always zero.
-__device__ __forceinline__ uint4 ctx_pixel(const Problem& pb, int qx, int qy, int visCur) {
-  if ((unsigned)qx >= (unsigned)pb.tw || (unsigned)qy >= (unsigned)pb.th) return make_uint4(0, 0, 0, 0);
+// The pixel's words, loaded without waiting on one another.
+struct CtxWords {
+  uint32_t px, map;
+  bool in, valued;
+};
+
+__device__ __forceinline__ CtxWords ctx_load(const Problem& pb, int qx, int qy, int visCur) {
+  CtxWords w{0u, 0u, false, false};
+  if ((unsigned)qx >= (unsigned)pb.tw || (unsigned)qy >= (unsigned)pb.th) return w;
   const int qi = qy * pb.tw + qx;
-  const bool valued = pb.vis ? pb.vis[qi] < visCur : pb.has[qi] != 0;
+  w.in = true;
+  w.valued = pb.vis ? __ldg(pb.vis + qi) < visCur : __ldg(pb.has + qi) != 0;
+  w.px = __ldg(pb.tpx + qi);
+  w.map = (pb.nm > 0 && pb.tmap) ? __ldg(pb.tmap + qi) : 0u;
+  return w;
+}
+
+__device__ __forceinline__ uint4 ctx_encode(const Problem& pb, const CtxWords& w) {
+  if (!w.in) return make_uint4(0, 0, 0, 0);
   float c0 = 0.f, c1 = 0.f, c2 = 0.f, h = 0.f, m = 0.f;
-  if (valued) {
-    const uint32_t p = pb.tpx[qi];
+  if (w.valued) {
     const int n1 = min(1, pb.nc - 1), n2 = min(2, pb.nc - 1);
-    c0 = (float)((p >> 8) & 0xFFu) / 255.f - 0.5f;
-    c1 = (float)((p >> (8 + 8 * n1)) & 0xFFu) / 255.f - 0.5f;
-    c2 = (float)((p >> (8 + 8 * n2)) & 0xFFu) / 255.f - 0.5f;
+    c0 = (float)((w.px >> 8) & 0xFFu) / 255.f - 0.5f;
+    c1 = (float)((w.px >> (8 + 8 * n1)) & 0xFFu) / 255.f - 0.5f;
+    c2 = (float)((w.px >> (8 + 8 * n2)) & 0xFFu) / 255.f - 0.5f;
     h = 1.f;
   }
-  if (pb.nm > 0 && pb.tmap) m = (float)(pb.tmap[qi] & 0xFFu) / 255.f - 0.5f;
+  if (pb.nm > 0 && pb.tmap) m = (float)(w.map & 0xFFu) / 255.f - 0.5f;
   return make_uint4(bf2(c0, c1), bf2(c2, h), bf2(m, 0.f), 0u);
+}
+
+__device__ __forceinline__ uint4 ctx_pixel(const Problem& pb, int qx, int qy, int visCur) {
+  return ctx_encode(pb, ctx_load(pb, qx, qy, visCur));
 }
 
 // --------------------------------------------------- fused inference kernel
@@ -171,6 +189,89 @@ struct InferArgs {
   int2* props;             // [n x 16] proposed sources, or null
   unsigned* err;           // bit 3: a wait ran out
 };
+
+// One layer of the fused forward for the kS contexts of a group: one thread
+// issues the layer's MMAs (tiles x 9 taps x K steps, descriptors advanced by
+// plain adds: the start-address field is byte address / 16), all threads
+// read their TMEM lane and write bias + ReLU (bf16) into the next layer's
+// slabs, or decode the head.  False when the MMA wait ran out.
+template <int L, bool FROM_PROBLEM>
+__device__ __forceinline__ bool infer_layer(const InferArgs& a, unsigned char* in, unsigned char* outb,
+                                            const uint16_t* sW, const float* sBias, uint32_t tmem,
+                                            uint64_t* barMma, uint32_t& phase, int g, int sv, int n0) {
+  constexpr int win = win_of(L), wout = win - 2, cin = cin_of(L), kst = cin / 16, tiles = tiles_of(L);
+  constexpr int inPad = pad_of(L);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    constexpr uint32_t idesc = tc::instr_desc(128, 32);
+    const uint64_t aBase = tc::smem_desc(tc::saddr(in), inPad * 16, 128);
+    const uint64_t bBase = tc::smem_desc(tc::saddr(sW + wblk_off(L)), 512, 128);
+#pragma unroll 1
+    for (int t = 0; t < tiles; t++) {
+#pragma unroll
+      for (int tap = 0; tap < 9; tap++) {
+        const int shift = (tap / 3) * win + tap % 3;
+#pragma unroll
+        for (int ks = 0; ks < kst; ks++) {
+          const uint64_t da = aBase + (uint64_t)(2 * ks * inPad + t * 128 + shift);
+          const uint64_t db = bBase + (uint64_t)(((tap * cin + 16 * ks) / 8) * 32);
+          tc::mma_bf16(tmem + t * 32, da, db, idesc, (tap | ks) ? 1u : 0u);
+        }
+      }
+    }
+    tc::mma_commit(barMma);
+  }
+  bool done = tc::mbar_wait(barMma, phase, 1 << 20);
+  phase ^= 1u;
+  done = __syncthreads_and(done) != 0;
+  if (!done) return false;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+  for (int t = 0; t < tiles; t++) {
+    uint32_t v[32];
+    tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * 32), v);
+    const int r = t * 128 + warp * 32 + lane;
+    const int b = r / (win * win), yx = r - b * win * win, y = yx / win, x = yx - y * win;
+    if (b >= sv || y >= wout || x >= wout) continue;
+    if (L < kLayers - 1) {
+      constexpr int outPad = L < kLayers - 1 ? pad_of(L + 1) : 0;
+      const int ro = (b * wout + y) * wout + x;
+      const float* bias = sBias + L * 32;
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int c = q * 8 + 2 * j;
+          w[j] = bf2(fmaxf(__uint_as_float(v[c]) + bias[c], 0.f), fmaxf(__uint_as_float(v[c + 1]) + bias[c + 1], 0.f));
+        }
+        *reinterpret_cast<uint4*>(outb + q * outPad * 16 + ro * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    } else {
+      const int s = g + b;
+      const float* bias = sBias + 4 * 32;
+      if (a.out) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) a.out[(size_t)s * 32 + j] = __uint_as_float(v[j]) + bias[j];
+      }
+      if (a.props) {
+        const int2 pos = FROM_PROBLEM ? a.targets[n0 + s] : make_int2(0, 0);
+#pragma unroll
+        for (int k = 0; k < kOffsets; k++) {
+          const float dx = (__uint_as_float(v[2 * k]) + bias[2 * k]) * kLabelScale;
+          const float dy = (__uint_as_float(v[2 * k + 1]) + bias[2 * k + 1]) * kLabelScale;
+          a.props[(size_t)s * kOffsets + k] = make_int2(pos.x + (int)fmaxf(fminf(rintf(dx), 1e8f), -1e8f),
+                                                        pos.y + (int)fmaxf(fminf(rintf(dy), 1e8f), -1e8f));
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  return true;
+}
 
 // Activation slab layout: for each 8-channel block q, `pad` rows of 16 bytes;
 // row = (sample, y, x) on the layer's own grid.  Row-major in one block makes
@@ -212,101 +313,56 @@ __global__ void __launch_bounds__(128, 1) k_net_infer(InferArgs a) {
   uint32_t phase = 0;
   for (int g = blockIdx.x * kS; ok && g < count; g += gridDim.x * kS) {
     const int sv = min(kS, count - g);
-    // layer-0 input: contexts of samples g .. g + sv
-    for (int r = tid; r < kS * 121; r += 128) {
-      const int b = r / 121, yx = r - b * 121;
-      uint4 lo = make_uint4(0, 0, 0, 0), hi = make_uint4(0, 0, 0, 0);
-      if (b < sv) {
-        if (FROM_PROBLEM) {
-          const int2 pos = a.targets[n0 + g + b];
-          const int y = yx / 11, x = yx - y * 11;
-          lo = ctx_pixel(a.pb, pos.x + x - 5, pos.y + y - 5, a.visCur);
-        } else {
-          const uint4* src = reinterpret_cast<const uint4*>(a.x0 + ((size_t)(g + b) * 121 + yx) * 16);
-          lo = src[0];
-          hi = src[1];
+    // layer-0 input: contexts of samples g .. g + sv.  Channels 8-15 (slab
+    // 1) are zero for contexts built here.  Rows go four at a time so that
+    // their loads are in flight together.
+    constexpr int kRows = kS * 121, kUnroll = 4;
+#pragma unroll 1
+    for (int base = 0; base < kRows; base += 128 * kUnroll) {
+      if (FROM_PROBLEM) {
+        CtxWords w[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++) {
+          const int r = base + u * 128 + tid, b = r / 121, yx = r - b * 121;
+          w[u] = CtxWords{0u, 0u, false, false};
+          if (r < kRows && b < sv) {
+            const int2 pos = a.targets[n0 + g + b];
+            const int y = yx / 11, x = yx - y * 11;
+            w[u] = ctx_load(a.pb, pos.x + x - 5, pos.y + y - 5, a.visCur);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++) {
+          const int r = base + u * 128 + tid;
+          if (r < kRows) {
+            *reinterpret_cast<uint4*>(buf0 + r * 16) = ctx_encode(a.pb, w[u]);
+            *reinterpret_cast<uint4*>(buf0 + pad_of(0) * 16 + r * 16) = make_uint4(0, 0, 0, 0);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++) {
+          const int r = base + u * 128 + tid, b = r / 121, yx = r - b * 121;
+          if (r >= kRows) continue;
+          uint4 lo = make_uint4(0, 0, 0, 0), hi = make_uint4(0, 0, 0, 0);
+          if (b < sv) {
+            const uint4* src = reinterpret_cast<const uint4*>(a.x0 + ((size_t)(g + b) * 121 + yx) * 16);
+            lo = src[0];
+            hi = src[1];
+          }
+          *reinterpret_cast<uint4*>(buf0 + r * 16) = lo;
+          *reinterpret_cast<uint4*>(buf0 + pad_of(0) * 16 + r * 16) = hi;
         }
       }
-      *reinterpret_cast<uint4*>(buf0 + r * 16) = lo;
-      *reinterpret_cast<uint4*>(buf0 + pad_of(0) * 16 + r * 16) = hi;
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-#pragma unroll
-    for (int l = 0; l < kLayers; l++) {
-      const int win = win_of(l), wout = win - 2, cin = cin_of(l), kst = cin / 16, tiles = tiles_of(l);
-      const int inPad = pad_of(l);
-      unsigned char* in = (l & 1) ? buf1 : buf0;
-      unsigned char* outb = (l & 1) ? buf0 : buf1;
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t idesc = tc::instr_desc(128, 32);
-        const uint32_t inAddr = tc::saddr(in), wAddr = tc::saddr(sW + wblk_off(l));
-        for (int t = 0; t < tiles; t++)
-          for (int tap = 0; tap < 9; tap++) {
-            const int shift = (tap / 3) * win + tap % 3;
-            for (int ks = 0; ks < kst; ks++) {
-              const uint64_t da =
-                  tc::smem_desc(inAddr + (uint32_t)(2 * ks * inPad * 16 + (t * 128 + shift) * 16), inPad * 16, 128);
-              const int kb = (tap * cin + 16 * ks) / 8;
-              const uint64_t db = tc::smem_desc(wAddr + kb * 512, 512, 128);
-              tc::mma_bf16(tmem + t * 32, da, db, idesc, (tap | ks) ? 1u : 0u);
-            }
-          }
-        tc::mma_commit(&barMma);
-      }
-      bool done = tc::mbar_wait(&barMma, phase, 1 << 20);
-      phase ^= 1u;
-      done = __syncthreads_and(done) != 0;
-      if (!done) {
-        if (tid == 0) atomicOr(a.err, 8u);
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int outPad = l < kLayers - 1 ? pad_of(l + 1) : 0;
-      for (int t = 0; t < tiles; t++) {
-        uint32_t v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(t * 32), v);
-        const int r = t * 128 + warp * 32 + lane;
-        const int b = r / (win * win), yx = r - b * win * win, y = yx / win, x = yx - y * win;
-        if (b >= sv || y >= wout || x >= wout) continue;
-        if (l < kLayers - 1) {
-          const int ro = (b * wout + y) * wout + x;
-          const float* bias = sBias + l * 32;
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            uint32_t w[4];
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-              const int c = q * 8 + 2 * j;
-              w[j] = bf2(fmaxf(__uint_as_float(v[c]) + bias[c], 0.f), fmaxf(__uint_as_float(v[c + 1]) + bias[c + 1], 0.f));
-            }
-            *reinterpret_cast<uint4*>(outb + q * outPad * 16 + ro * 16) = make_uint4(w[0], w[1], w[2], w[3]);
-          }
-        } else {
-          const int s = g + b;
-          const float* bias = sBias + 4 * 32;
-          if (a.out) {
-#pragma unroll
-            for (int j = 0; j < 32; j++) a.out[(size_t)s * 32 + j] = __uint_as_float(v[j]) + bias[j];
-          }
-          if (a.props) {
-            const int2 pos = FROM_PROBLEM ? a.targets[n0 + s] : make_int2(0, 0);
-#pragma unroll
-            for (int k = 0; k < kOffsets; k++) {
-              const float dx = (__uint_as_float(v[2 * k]) + bias[2 * k]) * kLabelScale;
-              const float dy = (__uint_as_float(v[2 * k + 1]) + bias[2 * k + 1]) * kLabelScale;
-              a.props[(size_t)s * kOffsets + k] =
-                  make_int2(pos.x + (int)fmaxf(fminf(rintf(dx), 1e8f), -1e8f), pos.y + (int)fmaxf(fminf(rintf(dy), 1e8f), -1e8f));
-            }
-          }
-        }
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncthreads();
-    }
+    ok = infer_layer<0, FROM_PROBLEM>(a, buf0, buf1, sW, sBias, tmem, &barMma, phase, g, sv, n0) &&
+         infer_layer<1, FROM_PROBLEM>(a, buf1, buf0, sW, sBias, tmem, &barMma, phase, g, sv, n0) &&
+         infer_layer<2, FROM_PROBLEM>(a, buf0, buf1, sW, sBias, tmem, &barMma, phase, g, sv, n0) &&
+         infer_layer<3, FROM_PROBLEM>(a, buf1, buf0, sW, sBias, tmem, &barMma, phase, g, sv, n0) &&
+         infer_layer<4, FROM_PROBLEM>(a, buf0, buf1, sW, sBias, tmem, &barMma, phase, g, sv, n0);
+    if (!ok && tid == 0) atomicOr(a.err, 8u);
   }
   // A failed weight wait may leave the copies in flight: wait once more.
   if (!ok) tc::mbar_wait(&barW, 0, 1 << 20);

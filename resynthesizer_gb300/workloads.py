@@ -72,6 +72,26 @@ def value_noise(h: int, w: int, channels: int, rng: SplitMix64, stripes: bool = 
     return out
 
 
+def value_noise_fast(h: int, w: int, channels: int, rng: SplitMix64) -> np.ndarray:
+    """value_noise (no stripes) in float64 through sin(a + b) = sin a cos b +
+    cos a sin b: two 1-D evaluations and an outer product per octave, the same
+    draws in the same order; for large images."""
+    x = np.arange(w, dtype=np.float64)
+    y = np.arange(h, dtype=np.float64)
+    out = np.empty((h, w, channels), np.uint8)
+    for c in range(channels):
+        v = np.full((h, w), 128.0)
+        for o in range(4):
+            th, ph = rng.uniform(2, 0.0, 2 * math.pi)
+            f = 2 * math.pi * (4 * 2 ** o) / w
+            ax = f * math.cos(th) * x
+            by = f * math.sin(th) * y + ph
+            v += (48.0 / 2 ** o) * (np.outer(np.cos(by), np.sin(ax)) + np.outer(np.sin(by), np.cos(ax)))
+        v += rng.uniform(h * w, -16.0, 16.0).reshape(h, w)
+        out[..., c] = np.clip(v, 0, 255).astype(np.uint8)
+    return out
+
+
 def value_noise_separable(h: int, w: int, channels: int, rng: SplitMix64) -> np.ndarray:
     """value_noise's distribution, computed with sin(a + b) = sin a cos b + cos a sin b
     so each octave costs two 1-D trig evaluations and one outer product."""
@@ -130,21 +150,25 @@ def ellipse_mask_fast(h: int, w: int, rng: SplitMix64, count: int, rmin: float, 
 def ellipse_mask(h: int, w: int, rng: SplitMix64, count: int, rmin: float, rmax: float,
                  lo_frac: float, hi_frac: float, rects: bool = False) -> np.ndarray:
     """Union of random ellipses (or rectangles), redrawn until the area lies in
-    [lo_frac, hi_frac]."""
-    y, x = np.mgrid[0:h, 0:w].astype(np.float32)
+    [lo_frac, hi_frac].  Each shape is evaluated only inside its bounding box
+    (it covers no pixel outside it)."""
     for _ in range(200):
         m = np.zeros((h, w), bool)
         for _ in range(count):
             cx, cy = rng.uniform(1, 0, w)[0], rng.uniform(1, 0, h)[0]
             rx, ry = rng.uniform(2, rmin, rmax)
+            r = max(rx, ry)
+            x0, x1 = max(0, int(cx - r) - 1), min(w, int(cx + r) + 2)
+            y0, y1 = max(0, int(cy - r) - 1), min(h, int(cy + r) + 2)
+            y, x = np.mgrid[y0:y1, x0:x1].astype(np.float32)
             if rects and rng.uniform(1)[0] < 0.5:
-                m |= (np.abs(x - cx) < rx) & (np.abs(y - cy) < ry)
+                m[y0:y1, x0:x1] |= (np.abs(x - cx) < rx) & (np.abs(y - cy) < ry)
             else:
                 a = rng.uniform(1, 0, math.pi)[0]
                 ca, sa = math.cos(a), math.sin(a)
                 u = (x - cx) * ca + (y - cy) * sa
                 v = -(x - cx) * sa + (y - cy) * ca
-                m |= (u / rx) ** 2 + (v / ry) ** 2 <= 1.0
+                m[y0:y1, x0:x1] |= (u / rx) ** 2 + (v / ry) ** 2 <= 1.0
         frac = m.mean()
         if lo_frac <= frac <= hi_frac:
             return np.where(m, 255, 0).astype(np.uint8)
@@ -209,7 +233,7 @@ def render1024(index: int = 0) -> dict:
 
 def heal4096(index: int = 0, size: int = 4096) -> dict:
     rng = SplitMix64(1000 * 2 + index)
-    img = value_noise(size, size, 3, rng)
+    img = value_noise_fast(size, size, 3, rng)
     scale = size / 4096.0
     mask = ellipse_mask(size, size, rng, 40, 20 * scale, 200 * scale, 0.09, 0.11)
     return dict(name=f"heal{size}", image=img, mask=mask, fmt=T_RGB,
