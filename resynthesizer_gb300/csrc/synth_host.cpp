@@ -504,6 +504,27 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
 
 // Radius (squared) of the offset list used by the wavefront mode: enough for
 // any dense patch; sparse early batches look this far for context.
+unsigned ilog2(uint64_t v) {
+  unsigned r = 0;
+  while (v >>= 1) r++;
+  return r;
+}
+
+// Autotuned warps per CTA by problem class (0 = not tuned yet).
+std::mutex g_tuneMu;
+std::map<uint64_t, int> g_tunedWarps;
+
+int tuned_warps(uint64_t key) {
+  std::lock_guard<std::mutex> lock(g_tuneMu);
+  auto it = g_tunedWarps.find(key);
+  return it == g_tunedWarps.end() ? 0 : it->second;
+}
+
+void set_tuned_warps(uint64_t key, int warps) {
+  std::lock_guard<std::mutex> lock(g_tuneMu);
+  g_tunedWarps[key] = warps;
+}
+
 long long wave_radius2(int w, int h) {
   const long long full = (long long)(w - 1) * (w - 1) + (long long)(h - 1) * (h - 1);
   return std::min<long long>(full, 256LL * 256LL);
@@ -739,6 +760,18 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     }
     rs::Counters& hc = *st.hostCtr;
     LaunchTimer prof;
+    // Warps per CTA: the caller's choice, or autotuned per problem class
+    // (colour and map channels, patch size, corpus and target sizes): the
+    // first refinement pass of a class times its first three batches with
+    // 16, 8 and 4 warps and the fastest serves every later launch of the
+    // class.  The result does not depend on the choice (exact minimum).
+    const uint64_t tuneKey = (uint64_t)dp.pb.nc | (uint64_t)(dp.pb.nm > 0) << 2 | (uint64_t)dp.pb.patchLimit << 4 |
+                             (uint64_t)ilog2((uint64_t)cw * ch) << 12 | (uint64_t)ilog2(ntargets) << 18;
+    int warps = opt.warpsPerBlock ? (int)opt.warpsPerBlock : tuned_warps(tuneKey);
+    const bool autoWarps = opt.warpsPerBlock == 0 && warps == 0;
+    if (!warps) warps = 16;
+    static const int kTryWarps[3] = {16, 8, 4};
+    cudaEvent_t tev[4] = {};
     for (int pass = 0; pass < rs::kPasses; pass++) {
       const unsigned end = ends[pass];
       // Bands of the visit order (rank thresholds): pass 0 grows
@@ -790,8 +823,22 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       const int nbatches = nb * k * k;
       wa.pass = (unsigned)pass;
       wa.sparse = (pass == 0 && sparseOk) ? 1 : 0;
+      const bool tuning = autoWarps && pass == 1 && nbatches >= 3;
+      if (tuning)
+        for (auto& e : tev) CK(cudaEventCreate(&e));
+      int maxCtas = 0, maxCommit = 0;
       for (int b = 0; b < nbatches; b++) {
         if (!phased[b / (k * k)] && b % (k * k)) continue;   // empty by construction
+        if (b % (k * k) == 0) {
+          // Grid cap from the band's expected batch size (its targets spread
+          // over k * k phases; twice that for the spread): small batches get
+          // one CTA per target instead of a persistent grid of idle CTAs.
+          const int band = b / (k * k);
+          const long long count = bandEnds[band] - (band ? bandEnds[band - 1] : 0);
+          const long long expect = 2 * ((count + k * k - 1) / (k * k)) + 4;
+          maxCtas = expect < 1 << 20 ? (int)expect : 0;
+          maxCommit = (int)std::min<long long>(1 << 20, expect / 256 + 1);
+        }
         if (net && b % (k * k) == 0) {
           const int band = b / (k * k);
           const int count = bandEnds[band] - (band ? bandEnds[band - 1] : 0);
@@ -803,20 +850,33 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
         }
         wa.batch = b;
         wa.visCur = pass == 0 ? b : 0x7ffffffe;
+        const int w = tuning && b < 3 ? kTryWarps[b] : warps;
+        if (tuning && b < 3) CK(cudaEventRecord(tev[b], s));
         if (opt.profile) prof.begin(s);
-        CK(rs_launch_wave(wa, (int)opt.warpsPerBlock, s));
+        CK(rs_launch_wave(wa, w, maxCtas, s));
         if (opt.profile) prof.end(s);
         launches++;
         if (!wa.inPlace) {
-          CK(rs_launch_commit(wa, s));
+          CK(rs_launch_commit(wa, maxCommit, s));
           launches++;
         }
+        if (tuning && b == 2) CK(cudaEventRecord(tev[3], s));
       }
       CK(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(st.hostInts + 3, batchStart + nbatches, sizeof(int), cudaMemcpyDeviceToHost, s));
       CK(cudaEventRecord(epass, s));
       wait_stream(st, epass, cancel);
       if (hc.error) return fail(RESYNTH_ERROR_DEVICE, "wavefront kernel reported error %u", hc.error);
+      if (tuning) {
+        float t[3];
+        for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&t[i], tev[i], tev[i + 1]));
+        int best = 0;
+        for (int i = 1; i < 3; i++)
+          if (t[i] < 0.97f * t[best]) best = i;
+        set_tuned_warps(tuneKey, kTryWarps[best]);
+        warps = kTryWarps[best];
+        for (auto& e : tev) cudaEventDestroy(e);
+      }
       const unsigned visited = (unsigned)st.hostInts[3];
       // callbacks the reference makes during this pass (lib/synthesize.h:493)
       for (unsigned t = 0; t < end; t += 4096u) prog.tick();

@@ -118,8 +118,8 @@ cudaError_t rs_launch_pack_padded(const uint8_t* raw, int w, int h, int bpp, int
 cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc, const uint32_t* px,
                                     cudaStream_t s);
 cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream_t s);
-cudaError_t rs_launch_wave(const rs::WaveArgs& a, int warpsPerBlock, cudaStream_t s);
-cudaError_t rs_launch_commit(const rs::WaveArgs& a, cudaStream_t s);
+cudaError_t rs_launch_wave(const rs::WaveArgs& a, int warpsPerBlock, int maxCtas, cudaStream_t s);
+cudaError_t rs_launch_commit(const rs::WaveArgs& a, int maxCtas, cudaStream_t s);
 cudaError_t rs_launch_frozen(const rs::ScoreArgs& a, cudaStream_t s);
 cudaError_t rs_launch_energy(const rs::ScoreArgs& a, cudaStream_t s);
 cudaError_t rs_prep_target(const uint8_t* raw, int w, int h, int bpp, int alpha, int hasAlpha, int useContext,

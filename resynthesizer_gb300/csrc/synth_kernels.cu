@@ -1133,7 +1133,7 @@ size_t wave_smem(const Problem& pb, bool smemc, int warps) {
 }
 
 template <int NC, bool MAP, bool SMEMC>
-cudaError_t launch_wave_t(const WaveArgs& a, int warps, size_t smem, cudaStream_t s) {
+cudaError_t launch_wave_t(const WaveArgs& a, int warps, int maxCtas, size_t smem, cudaStream_t s) {
   auto kern = k_wave<NC, MAP, SMEMC>;
   // Per-instantiation launch configuration, shared by all host threads.
   static std::mutex mu;
@@ -1156,13 +1156,16 @@ cudaError_t launch_wave_t(const WaveArgs& a, int warps, size_t smem, cudaStream_
     }
   }
   if (perSm < 1) return cudaErrorInvalidConfiguration;
-  // Persistent grid: the batch size is only known on the device.
-  kern<<<sm_count() * perSm, warps * 32, smem, s>>>(a);
+  // Persistent grid (the batch size is only known on the device), capped by
+  // the caller's estimate for small batches so that idle CTAs are not launched.
+  int grid = sm_count() * perSm;
+  if (maxCtas > 0) grid = std::min(grid, maxCtas);
+  kern<<<grid, warps * 32, smem, s>>>(a);
   return cudaGetLastError();
 }
 }  // namespace
 
-extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, cudaStream_t s) {
+extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, int maxCtas, cudaStream_t s) {
   if (warps < 1) warps = 16;
   if (warps > 16) warps = 16;
   const size_t smemCorpus = wave_smem(a.pb, true, warps);
@@ -1170,15 +1173,17 @@ extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, cudaStream_t
   const size_t smem = smemc ? smemCorpus : wave_smem(a.pb, false, warps);
   cudaError_t e = cudaSuccess;
   if (smemc) {
-    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, true>(a, warps, smem, s)));
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, true>(a, warps, maxCtas, smem, s)));
   } else {
-    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, false>(a, warps, smem, s)));
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, false>(a, warps, maxCtas, smem, s)));
   }
   return e;
 }
 
-extern "C" cudaError_t rs_launch_commit(const WaveArgs& a, cudaStream_t s) {
-  k_commit<<<sm_count() * 2, 256, 0, s>>>(a);
+extern "C" cudaError_t rs_launch_commit(const WaveArgs& a, int maxCtas, cudaStream_t s) {
+  int grid = sm_count() * 2;
+  if (maxCtas > 0) grid = std::min(grid, maxCtas);
+  k_commit<<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
