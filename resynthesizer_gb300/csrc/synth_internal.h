@@ -92,6 +92,7 @@ struct WaveArgs {
   const int2* props;             // proposal network's sources, 16 per target of the band, or null
   int nprop;                     // how many of each target's 16 are scored
   int propBatch0;                // the band's first batch: props index = t - batchStart[propBatch0]
+  int probeShare;                // random probes keyed by (batch, slot / 16) instead of the pixel
 };
 
 // Frozen-state scoring and energy.
@@ -120,6 +121,7 @@ cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc,
 cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream_t s);
 cudaError_t rs_launch_wave(const rs::WaveArgs& a, int warpsPerBlock, int maxCtas, cudaStream_t s);
 cudaError_t rs_launch_commit(const rs::WaveArgs& a, int maxCtas, cudaStream_t s);
+int rs_wave_corpus_staged(const rs::Problem& pb, int warps);
 cudaError_t rs_launch_frozen(const rs::ScoreArgs& a, cudaStream_t s);
 cudaError_t rs_launch_energy(const rs::ScoreArgs& a, cudaStream_t s);
 cudaError_t rs_prep_target(const uint8_t* raw, int w, int h, int bpp, int alpha, int hasAlpha, int useContext,
@@ -130,6 +132,7 @@ int rs_prep_scratch_ints(int w, int h);
 cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
                             const int* dBandEnds, const int* dBandPhased, int nbands, int k, int* work,
                             int* batchStart, int2* out, int* vis, cudaStream_t s);
+size_t rs_prep_batches_ints(int n, int nkeys);
 cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, size_t maskRow, const uint8_t* mask2,
                      size_t mask2Row, int w, int h, int bpp, uint8_t* target, uint8_t* corpus, cudaStream_t s);
 cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow, cudaStream_t s);

@@ -905,7 +905,13 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
     // one is replaced by an extra probe), then the random probes.
     const int nprop = a.props ? a.nprop : 0;
     const int ncand = np + nprop + (int)a.trys;
-    const uint32_t pbase = probe_base(a.seed, a.pass, (uint32_t)pi);
+    // Probe keys: per target pixel, or shared by 16 consecutive slots of the
+    // batch (neighbours in the target list, which the batches keep in order):
+    // the warps of a CTA then read the same random corpus windows, which stay
+    // in L1/L2 when the corpus itself is too large to.
+    const uint32_t pbase = a.probeShare
+                               ? probe_base(a.seed ^ 0x6A09E667u, a.pass, (uint32_t)a.batch * 0x01000193u + ((uint32_t)slot >> 4))
+                               : probe_base(a.seed, a.pass, (uint32_t)pi);
     const int2* myProps = nprop ? a.props + (size_t)(t - a.batchStart[a.propBatch0]) * 16 : nullptr;
     auto cand = [&](int k) -> int2 {
       if (k < np) return prop[k];
@@ -1178,6 +1184,11 @@ extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, int maxCtas,
     RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, false>(a, warps, maxCtas, smem, s)));
   }
   return e;
+}
+
+extern "C" int rs_wave_corpus_staged(const Problem& pb, int warps) {
+  if (warps < 1 || warps > 16) warps = 16;
+  return wave_smem(pb, true, warps) <= 112 * 1024 ? 1 : 0;
 }
 
 extern "C" cudaError_t rs_launch_commit(const WaveArgs& a, int maxCtas, cudaStream_t s) {

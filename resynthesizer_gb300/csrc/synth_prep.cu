@@ -145,61 +145,127 @@ __global__ void k_compact(PixPred pred, int npx, int w, const int* blockOffsets,
   }
 }
 
+// Targets per bucketing chunk: one CTA each, so the result does not depend
+// on the grid.
+constexpr int kBucketChunk = 8192;
+
 // Batch keys of one pass.  rank = position in the visit order: given (the
 // host order) or drawn from a hash of the pixel (random orders).  Targets of
-// rank >= endRank are not visited this pass.  key = band * K + phase.
-// Warp-aggregated atomicAdd of 1 on counter[key] (key < 0: no-op): one
-// atomic per distinct key in the warp; returns the old value plus this
-// lane's rank among the lanes sharing its key.
-__device__ __forceinline__ int warp_bump(int* counter, int key) {
-  const unsigned peers = __match_any_sync(0xffffffffu, key);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  int base = 0;
-  if (lane == leader && key >= 0) base = atomicAdd(&counter[key], __popc(peers));
-  base = __shfl_sync(0xffffffffu, base, leader);
+// rank >= endRank are not visited this pass.  key = band * K + phase.  Each
+// CTA counts its chunk's keys; counts are stored key-major, [key][chunk], so
+// one exclusive scan gives every (key, chunk) its output position.
+__global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
+                             const int* bandEnds, const int* bandPhased, int nbands, int k, int* keys, int* counts,
+                             int nchunks, int* vis) {
+  extern __shared__ int hist[];
+  const int nkeys = nbands * k * k;
+  for (int i = threadIdx.x; i < nkeys; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  const int chunk = blockIdx.x;
+  for (int i = threadIdx.x; i < kBucketChunk; i += blockDim.x) {
+    const int t = chunk * kBucketChunk + i;
+    if (t >= n) break;
+    const int2 p = targets[t];
+    const int rank = randomOrder ? (int)__umulhi(mix32p((uint32_t)(p.y * tw + p.x) * 0x9E3779B1u ^ seed),
+                                                 (uint32_t)n)
+                                 : t;
+    int key = -1;
+    if (rank < endRank) {
+      int band = 0;
+      while (band < nbands - 1 && rank >= bandEnds[band]) band++;
+      key = band * k * k + (bandPhased[band] ? (p.y % k) * k + (p.x % k) : 0);
+      atomicAdd(&hist[key], 1);
+    }
+    keys[t] = key;
+    // pass 0: the pixel gets its value in batch `key`
+    if (vis && key >= 0) vis[p.y * tw + p.x] = key;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nkeys; i += blockDim.x) counts[(size_t)i * nchunks + chunk] = hist[i];
+}
+
+// Exclusive scan of n ints by one CTA of 1024 threads, 8 consecutive
+// elements per thread per round; offsets[n] = the total.
+__global__ void __launch_bounds__(1024) k_scan_wide(const int* counts, int n, int* offsets) {
+  __shared__ int warpSums[32];
+  __shared__ int carry;
+  constexpr int kPer = 8;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += 1024 * kPer) {
+    const int i0 = base + threadIdx.x * kPer;
+    int v[kPer], sum = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+      v[j] = i0 + j < n ? counts[i0 + j] : 0;
+      sum += v[j];
+    }
+    int x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = warpSums[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warpSums[lane] = w;   // inclusive
+    }
+    __syncthreads();
+    int run = carry + (warp ? warpSums[warp - 1] : 0) + x - sum;
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+      if (i0 + j < n) offsets[i0 + j] = run;
+      run += v[j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warpSums[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) offsets[n] = carry;
+}
+
+// batchStart[key] = the scanned offset of (key, chunk 0).
+__global__ void k_batch_starts(const int* offsets, int nkeys, int nchunks, int* batchStart) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= nkeys; i += gridDim.x * blockDim.x)
+    batchStart[i] = offsets[(size_t)i * nchunks];
+}
+
+// Stable scatter: within a batch, targets keep their order in the target
+// list.  Each CTA places its chunk; a lane's position is its (key, chunk)
+// offset + the same-key count of earlier warps (taken warp by warp) + its
+// rank among the same-key lanes of its warp.
+__global__ void k_scatter(const int2* targets, int n, const int* keys, const int* offsets, int nkeys, int nchunks,
+                          int2* out) {
+  extern __shared__ int cnt[];
+  for (int i = threadIdx.x; i < nkeys; i += blockDim.x) cnt[i] = 0;
+  __syncthreads();
+  const int chunk = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   unsigned lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-  return base + __popc(peers & lt);
-}
-
-__global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
-                             const int* bandEnds, const int* bandPhased, int nbands, int k, int* keys, int* hist,
-                             int* vis) {
-  const int stride = gridDim.x * blockDim.x;
-  const int limit = (n + stride - 1) / stride * stride;   // whole warps iterate together
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < limit; t += stride) {
-    int key = -1;
-    if (t < n) {
-      const int2 p = targets[t];
-      const int rank = randomOrder ? (int)__umulhi(mix32p((uint32_t)(p.y * tw + p.x) * 0x9E3779B1u ^ seed),
-                                                   (uint32_t)n)
-                                   : t;
-      if (rank < endRank) {
-        int band = 0;
-        while (band < nbands - 1 && rank >= bandEnds[band]) band++;
-        key = band * k * k + (bandPhased[band] ? (p.y % k) * k + (p.x % k) : 0);
-      }
-      keys[t] = key;
-      // pass 0: the pixel gets its value in batch `key`
-      if (vis && key >= 0) vis[p.y * tw + p.x] = key;
-    }
-    warp_bump(hist, key);
-  }
-}
-
-__global__ void k_scatter(const int2* targets, int n, const int* keys, int* cursor, int2* out) {
-  const int stride = gridDim.x * blockDim.x;
-  const int limit = (n + stride - 1) / stride * stride;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < limit; t += stride) {
+  for (int base = 0; base < kBucketChunk; base += blockDim.x) {
+    const int t = chunk * kBucketChunk + base + threadIdx.x;
     const int key = t < n ? keys[t] : -1;
-    const int pos = warp_bump(cursor, key);
-    if (key >= 0) out[pos] = targets[t];
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    int before = 0;
+    for (int w = 0; w < nwarps; w++) {
+      if (warp == w) {
+        if (key >= 0) before = cnt[key];
+        __syncwarp();
+        if (lane == leader && key >= 0) cnt[key] = before + __popc(peers);
+      }
+      __syncthreads();
+    }
+    if (key >= 0) out[offsets[(size_t)key * nchunks + chunk] + before + __popc(peers & lt)] = targets[t];
   }
-}
-
-__global__ void k_copy_int(const int* a, int* b, int n) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = a[i];
 }
 
 int blocks_for(int n, int per) { return (n + per - 1) / per; }
@@ -243,21 +309,30 @@ extern "C" int rs_prep_scratch_ints(int w, int h) { return 2 * blocks_for(w * h,
 // Buckets the targets of one pass into batches: out[batchStart[b] ..
 // batchStart[b+1]) are the targets of batch b = band * k * k + phase.
 // work: 3 * nkeys + 1 + n ints.
+// Buckets the targets of one pass into batches: out[batchStart[b] ..
+// batchStart[b+1]) are the targets of batch b = band * k * k + phase, in the
+// order of the target list.  work: rs_prep_batches_ints(n, nkeys) ints.
 extern "C" cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder,
                                        uint32_t seed, const int* dBandEnds, const int* dBandPhased, int nbands,
                                        int k, int* work, int* batchStart, int2* out, int* vis, cudaStream_t s) {
   const int nkeys = nbands * k * k;
-  int* hist = work;
-  int* cursor = work + nkeys;
-  int* keys = work + 2 * nkeys + 1;
-  cudaMemsetAsync(hist, 0, sizeof(int) * nkeys, s);
-  const int g = std::min(blocks_for(n, 256), 1184);
-  k_batch_keys<<<g, 256, 0, s>>>(targets, n, tw, endRank, randomOrder, seed, dBandEnds, dBandPhased, nbands, k,
-                                 keys, hist, vis);
-  k_scan<<<1, kThreads, 0, s>>>(hist, nkeys, batchStart);
-  k_copy_int<<<blocks_for(nkeys, 256), 256, 0, s>>>(batchStart, cursor, nkeys);
-  k_scatter<<<g, 256, 0, s>>>(targets, n, keys, cursor, out);
+  const int nchunks = std::max(1, blocks_for(n, kBucketChunk));
+  const size_t cells = (size_t)nkeys * nchunks;
+  int* counts = work;
+  int* offsets = work + cells;
+  int* keys = work + 2 * cells + 1;
+  const size_t smem = (size_t)nkeys * sizeof(int);
+  k_batch_keys<<<nchunks, 256, smem, s>>>(targets, n, tw, endRank, randomOrder, seed, dBandEnds, dBandPhased, nbands,
+                                          k, keys, counts, nchunks, vis);
+  k_scan_wide<<<1, 1024, 0, s>>>(counts, (int)cells, offsets);
+  k_batch_starts<<<blocks_for(nkeys + 1, 256), 256, 0, s>>>(offsets, nkeys, nchunks, batchStart);
+  k_scatter<<<nchunks, 256, smem, s>>>(targets, n, keys, offsets, nkeys, nchunks, out);
   return cudaGetLastError();
+}
+
+extern "C" size_t rs_prep_batches_ints(int n, int nkeys) {
+  const size_t nchunks = (size_t)std::max(1, blocks_for(n, kBucketChunk));
+  return 2 * (size_t)nkeys * nchunks + 1 + (size_t)n;
 }
 
 namespace rs {
