@@ -157,6 +157,7 @@ typedef struct {
   unsigned int proposals;     /* wavefront: how many of the network's 16 offsets are scored (0 = none) */
   TResynthPairs *dumpPairs;   /* wavefront: append (context, final source) training pairs at the end */
   unsigned int dumpStride;    /* every dumpStride-th target of the visit order gives a pair (0 = 16) */
+  int graphs;                 /* wavefront: launch each pass as one captured CUDA graph */
 } TResynthOptions;
 
 typedef struct {

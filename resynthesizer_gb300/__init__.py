@@ -59,7 +59,8 @@ class Options(C.Structure):
     _fields_ = [("mode", C.c_int), ("seed", C.c_uint), ("firstBatch", C.c_uint), ("refineBatches", C.c_uint),
                 ("warpsPerBlock", C.c_uint), ("recordState", C.c_int), ("profile", C.c_int),
                 ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint),
-                ("net", C.c_void_p), ("proposals", C.c_uint), ("dumpPairs", C.c_void_p), ("dumpStride", C.c_uint)]
+                ("net", C.c_void_p), ("proposals", C.c_uint), ("dumpPairs", C.c_void_p), ("dumpStride", C.c_uint),
+                ("graphs", C.c_int)]
 
 
 class TrainOptions(C.Structure):
@@ -181,7 +182,7 @@ def format_indices(colors, mapColors=0, alphaTarget=0, alphaSource=0, isMap=0) -
 
 def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, recordState=0,
             profile=0, phaseSide=0, bandGrowth=0, minPasses=0, net=None, proposals=0, dump=None,
-            dumpStride=0) -> Options:
+            dumpStride=0, graphs=0) -> Options:
     o = Options()
     lib().resynthDefaultOptions(C.byref(o))
     if mode is not None:
@@ -193,6 +194,7 @@ def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, r
     o.proposals = proposals if net is not None else 0
     o.dumpPairs = dump.handle if dump is not None else None
     o.dumpStride = dumpStride
+    o.graphs = graphs
     return o
 
 

@@ -804,6 +804,12 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       CK(cudaMemcpyAsync(dBandEnds, bandEnds.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
       CK(cudaMemcpyAsync(dBandPhased, phased.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
       h2d += 2 * nb * sizeof(int);
+      // With graphs, the pass's launches (bucketing, cell minima, proposals,
+      // the batches) are captured and launched as one CUDA graph; timing and
+      // tuning passes use plain launches.
+      const bool tuningPass = autoWarps && pass == 1;
+      const bool graphPass = opt.graphs && !opt.profile && !tuningPass;
+      if (graphPass) CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       // Bucket this pass's targets by (band, colour phase): targets of one
       // phase are at least k apart, farther than a dense patch reaches, so
       // the targets of one batch never read each other.
@@ -868,10 +874,20 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
         }
         if (tuning && b == 2) CK(cudaEventRecord(tev[3], s));
       }
+      cudaGraphExec_t passExec = nullptr;
+      if (graphPass) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamEndCapture(s, &graph));
+        const cudaError_t ie = cudaGraphInstantiate(&passExec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(ie);
+        CK(cudaGraphLaunch(passExec, s));
+      }
       CK(cudaMemcpyAsync(&hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s));
       CK(cudaMemcpyAsync(st.hostInts + 3, batchStart + nbatches, sizeof(int), cudaMemcpyDeviceToHost, s));
       CK(cudaEventRecord(epass, s));
       wait_stream(st, epass, cancel);
+      if (passExec) cudaGraphExecDestroy(passExec);
       if (hc.error) return fail(RESYNTH_ERROR_DEVICE, "wavefront kernel reported error %u", hc.error);
       if (tuning) {
         float t[3];

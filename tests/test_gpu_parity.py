@@ -246,6 +246,22 @@ def test_cell_grid_patches_equal_offset_walk(density):
             assert np.array_equal(a[i], b[i]), (p, i)
 
 
+@pytest.mark.parametrize("case", ["render", "heal"])
+def test_wavefront_graphs_identical(case):
+    # each pass launched as one captured CUDA graph gives the same output
+    if case == "render":
+        wl = W.render(tile=32, out=160)
+        tgt, cor, spec, kw = wl["target"], wl["corpus"], wl["format"], wl["params"]
+    else:
+        wl = W.heal4096(index=1, size=256)
+        tgt, cor = W.simple_to_pixmaps(wl["image"], wl["mask"])
+        spec, kw = (3, 0, 0, 0, 0), wl["params"]
+    fmt = R.format_indices(*spec)
+    a = R.engine(tgt, cor, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=16))
+    b = R.engine(tgt, cor, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=16, graphs=1))
+    assert a.rc == b.rc == 0 and (a.out == b.out).all()
+
+
 def test_batch_matches_single_calls(oracle):
     # more than 16 distinct sizes across 4 workers: shared host caches get evicted while in use
     reqs = W.batch_requests(n=24, lo=40, hi=120, index=5)
