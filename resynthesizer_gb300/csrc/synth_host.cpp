@@ -411,6 +411,47 @@ std::shared_ptr<const std::vector<int2>> cached_offsets(int w, int h, long long 
   return list;
 }
 
+// The wavefront offset list: every offset within 256 px, in the sorted
+// offset list's order (ascending dx^2 + dy^2, ties by descending dy, then
+// descending dx).  That order does not depend on the box, so the wavefront
+// list of any image (radius min(box diagonal, 256)) is this one restricted to
+// |dx| < box width, |dy| < box height -- the kernels apply that restriction --
+// and one list, uploaded once per device, serves every image size.
+const std::vector<int2>& wave_offsets_host() {
+  static const std::vector<int2> list = sorted_offsets(257, 257, 256LL * 256LL);
+  return list;
+}
+
+const int2* wave_offsets_device(int& n) {
+  static std::mutex mu;
+  static std::map<int, int2*> perDevice;
+  const std::vector<int2>& host = wave_offsets_host();
+  n = (int)host.size();
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = perDevice.find(dev);
+  if (it != perDevice.end()) return it->second;
+  int2* d = nullptr;
+  CK(cudaMalloc(&d, host.size() * sizeof(int2)));
+  CK(cudaMemcpy(d, host.data(), host.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  perDevice[dev] = d;
+  return d;
+}
+
+// k of the colour phases: the reach of a dense patch (its last offset) + 1.
+int phase_side_box(const std::vector<int2>& offs, int patchLimit, int w, int h) {
+  int taken = 0;
+  int2 last = make_int2(0, 0);
+  for (const int2& o : offs) {
+    if (std::abs(o.x) >= w || std::abs(o.y) >= h) continue;
+    last = o;
+    if (++taken == patchLimit) break;
+  }
+  const double r = std::sqrt((double)last.x * last.x + (double)last.y * last.y);
+  return std::max(1, std::min(8, (int)std::floor(r) + 1));
+}
+
 struct RecordedState {
   std::vector<int2> src;
   std::vector<uint8_t> has;
@@ -444,7 +485,7 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
                            const uint8_t* dT, unsigned tw, unsigned th, const uint8_t* dC, unsigned cw, unsigned ch,
                            const uint8_t* hasInit, const int2* srcInit,
                            const std::vector<int2>& offs, long long maxD2, unsigned long long& h2d,
-                           unsigned& launches) {
+                           unsigned& launches, const int2* dOffs = nullptr, int nOffs = 0) {
   DeviceProblem d;
   rs::Problem& pb = d.pb;
   pb.tw = (int)tw;
@@ -489,8 +530,13 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
   pb.boxW = (int)std::min(tw, cw);
   pb.boxH = (int)std::min(th, ch);
   pb.maxD2 = maxD2;
-  pb.offs = ar.upload(offs.data(), offs.size(), h2d);
-  pb.noffs = (int)offs.size();
+  if (dOffs) {
+    pb.offs = dOffs;
+    pb.noffs = nOffs;
+  } else {
+    pb.offs = ar.upload(offs.data(), offs.size(), h2d);
+    pb.noffs = (int)offs.size();
+  }
   pb.patchLimit = (int)std::max(p.patchSize, 2u);
   pb.tileH = p.isMakeSeamlesslyTileableHorizontally ? 1 : 0;
   pb.tileV = p.isMakeSeamlesslyTileableVertically ? 1 : 0;
@@ -564,12 +610,6 @@ class LaunchTimer {
 // Side k of the colour phases: one more than the radius of a dense patch
 // (the distance of its last offset), so two targets of one phase are never
 // inside each other's dense patch.
-int phase_side(const std::vector<int2>& offs, int patchLimit) {
-  const size_t i = std::min<size_t>(offs.size(), (size_t)patchLimit) - 1;
-  const double r = std::sqrt((double)offs[i].x * offs[i].x + (double)offs[i].y * offs[i].y);
-  return std::max(1, std::min(8, (int)std::floor(r) + 1));
-}
-
 void wait_stream(Stream& st, cudaEvent_t ev, int* cancel) {
   while (true) {
     const cudaError_t q = cudaEventQuery(ev);
@@ -609,8 +649,21 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
   }
   const int mw = (int)std::min(tw, cw), mh = (int)std::min(th, ch);
   const long long maxD2 = replay ? LLONG_MAX : wave_radius2(mw, mh);
-  const auto offsHeld = cached_offsets(mw, mh, maxD2);
-  const std::vector<int2>& offs = *offsHeld;
+  // Replay walks the reference's full list of this box; the wavefront walks
+  // the shared device list restricted to the box.
+  const std::vector<int2> noList;
+  std::shared_ptr<const std::vector<int2>> offsHeld;
+  int nWave = 0;
+  const int2* dWave = replay ? nullptr : wave_offsets_device(nWave);
+  if (dWave) {
+    // only the prefix within this problem's radius (the list is sorted by d^2)
+    const std::vector<int2>& wl = wave_offsets_host();
+    nWave = (int)(std::partition_point(wl.begin(), wl.end(), [&](const int2& o) {
+                    return (long long)o.x * o.x + (long long)o.y * o.y <= maxD2;
+                  }) - wl.begin());
+  }
+  if (replay) offsHeld = cached_offsets(mw, mh, maxD2);
+  const std::vector<int2>& offs = replay ? *offsHeld : noList;
 
   Arena ar(s);
   unsigned long long h2d = 0;
@@ -621,7 +674,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
   CK(cudaEventCreateWithFlags(&epass, cudaEventDisableTiming));
   CK(cudaEventRecord(e0, s));
   DeviceProblem dp = make_problem(ar, s, p, f, dT, tw, th, dC, cw, ch, devicePrep ? nullptr : prepared->hasValue.data(),
-                                  nullptr, offs, maxD2, h2d, launches);
+                                  nullptr, offs, maxD2, h2d, launches, dWave, nWave);
   int2* dTargets = nullptr;
   unsigned ntargets = 0, ends[rs::kPasses], estimated = 0;
   bool noContext = true;
@@ -727,7 +780,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     const unsigned first = opt.firstBatch ? opt.firstBatch : (randomOrder ? 16u : 1024u);
     const unsigned refine = opt.refineBatches ? opt.refineBatches : 1u;
     const double growth = (opt.bandGrowth ? opt.bandGrowth : 200u) / 100.0;
-    const int k = opt.phaseSide ? (int)opt.phaseSide : phase_side(offs, dp.pb.patchLimit);
+    const int k = opt.phaseSide ? (int)opt.phaseSide : phase_side_box(wave_offsets_host(), dp.pb.patchLimit, mw, mh);
     constexpr int kMaxBands = 64;
     // While no pixel outside the current pass has a value, a batch's patches
     // can come from the list of already-synthesized targets (cheap when short).

@@ -110,7 +110,8 @@ __device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int
     if (j < noffs) {
       o = __ldg(&pb.offs[j]);
       int qx = px + o.x, qy = py + o.y;
-      if (wrap_or_clip(pb, qx, qy)) {
+      // the shared wavefront list spans every box: keep this box's offsets
+      if (abs(o.x) < pb.boxW && abs(o.y) < pb.boxH && wrap_or_clip(pb, qx, qy)) {
         qi = qy * pb.tw + qx;
         ok = pb.vis ? pb.vis[qi] < visCur : pb.has[qi] != 0;
       }
