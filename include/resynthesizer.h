@@ -158,6 +158,7 @@ typedef struct {
   TResynthPairs *dumpPairs;   /* wavefront: append (context, final source) training pairs at the end */
   unsigned int dumpStride;    /* every dumpStride-th target of the visit order gives a pair (0 = 16) */
   int graphs;                 /* wavefront: launch each pass as one captured CUDA graph */
+  int separateRequests;       /* imageSynthBatch: one stream per request instead of the many-request launches */
 } TResynthOptions;
 
 typedef struct {
@@ -286,9 +287,12 @@ typedef struct {
 } TResynthRequest;
 
 /* No counterpart in the reference (which heals one image per call).  Runs
- * `count` independent requests concurrently on `concurrency` host workers
- * (0 = 8), each with its own CUDA stream, so the small batches of many
- * requests overlap on the GPU.  Each request's result equals an imageSynthEx
+ * `count` independent requests of any sizes and formats.  In wavefront mode,
+ * requests with a random order (matchContextType 0 or 1) are synthesized
+ * together: each pass runs step b -- batch b of every request -- as one
+ * launch per pixel layout.  Other requests (and all of them with
+ * options->separateRequests) run on `concurrency` host workers (0 = 8), each
+ * with its own CUDA stream.  Each request's result equals an imageSynthEx
  * call with the same options.  stats (may be NULL) sums all requests.
  * Returns 0, or the first nonzero request result. */
 int imageSynthBatch(TResynthRequest *requests, unsigned int count, unsigned int concurrency,

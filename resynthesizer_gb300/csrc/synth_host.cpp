@@ -367,16 +367,31 @@ Stream& thread_stream() {
 }
 
 // Stream-ordered device allocations released at scope exit.
+// With a chunk size, allocations are carved out of large chunks so that the
+// buffers of many small problems sit close together in the address space
+// (fewer address-translation misses when one kernel touches all of them).
 class Arena {
  public:
-  explicit Arena(cudaStream_t s) : s_(s) {}
+  explicit Arena(cudaStream_t s, size_t chunk = 0) : s_(s), chunk_(chunk) {}
   ~Arena() {
     for (void* p : ptrs_) cudaFreeAsync(p, s_);
   }
   template <class T>
   T* alloc(size_t n) {
+    const size_t bytes = std::max<size_t>(n, 1) * sizeof(T) + 16;
+    if (chunk_ && bytes <= chunk_ / 4) {
+      const size_t need = (bytes + 255) & ~(size_t)255;
+      if (!cur_ || used_ + need > chunk_) {
+        CK(cudaMallocAsync(&cur_, chunk_, s_));
+        ptrs_.push_back(cur_);
+        used_ = 0;
+      }
+      void* p = static_cast<char*>(cur_) + used_;
+      used_ += need;
+      return static_cast<T*>(p);
+    }
     void* p = nullptr;
-    CK(cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T) + 16, s_));
+    CK(cudaMallocAsync(&p, bytes, s_));
     ptrs_.push_back(p);
     return static_cast<T*>(p);
   }
@@ -390,6 +405,8 @@ class Arena {
 
  private:
   cudaStream_t s_;
+  size_t chunk_ = 0, used_ = 0;
+  void* cur_ = nullptr;
   std::vector<void*> ptrs_;
 };
 
@@ -1003,6 +1020,330 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
   return 0;
 }
 
+// ------------------------------------------------- many requests at once
+// imageSynthBatch's wavefront path for requests with a random order: every
+// request is set up on one stream (device adaption, packing, device
+// preparation), then each pass buckets every request and runs step b -- batch
+// b of every request still active -- as one launch per pixel layout, the
+// requests' slots concatenated.  The per-request results equal single calls
+// (same batches, probes and patches; the minimum does not depend on the team
+// layout).
+
+struct BatchJob {
+  TResynthRequest* req = nullptr;
+  TImageSynthParameters p{};
+  TFormatIndices f{};
+  unsigned w = 0, h = 0, bpp = 0;
+  size_t imgBytes = 0;
+  uint8_t* dImg = nullptr;
+  uint8_t* dT = nullptr;
+  DeviceProblem dp;
+  int2* dTargets = nullptr;
+  int* dCounts = nullptr;
+  int2* cpts = nullptr;
+  unsigned ntargets = 0, ends[rs::kPasses] = {}, estimated = 0;
+  bool noContext = true, tiled = false, active = false;
+  int k = 1, cellsW = 0, cellsH = 0;
+  int* vis = nullptr;
+  int* cellMin = nullptr;
+  int* batchStart = nullptr;
+  int* work = nullptr;
+  int2* dPass = nullptr;
+  int* dBandEnds = nullptr;
+  int* dBandPhased = nullptr;
+  std::vector<int> bandEnds;
+  rs::WaveArgs wa{};
+  unsigned bettersTotal = 0, passes = 0;
+};
+
+bool batch_eligible(const TResynthRequest& r, const TResynthOptions& opt) {
+  if (opt.mode == RESYNTH_MODE_REPLAY || opt.net || opt.dumpPairs || opt.recordState || opt.profile) return false;
+  if (!r.image || !r.mask) return false;
+  const int ctx = r.parameters ? r.parameters->matchContextType : 1;
+  return ctx == 0 || ctx == 1;
+}
+
+int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& opt, TResynthStats& stats) {
+  Stream& st = thread_stream();
+  cudaStream_t s = st.s;
+  Arena ar(s, (size_t)256 << 20);
+  constexpr int kMaxBands = 64;
+  std::vector<BatchJob> jobs(reqs.size());
+  unsigned long long h2d = 0, d2h = 0;
+  unsigned launches = 0;
+  cudaEvent_t e0, e1, epass;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventCreateWithFlags(&epass, cudaEventDisableTiming));
+  CK(cudaEventRecord(e0, s));
+  *st.abortHost = 0;
+  // 1. host checks (the reference's order), upload, adaption, preparation
+  for (size_t i = 0; i < reqs.size(); i++) {
+    BatchJob& J = jobs[i];
+    TResynthRequest& R = *reqs[i];
+    J.req = &R;
+    R.result = 0;
+    if (R.image->width != R.mask->width || R.image->height != R.mask->height) {
+      R.result = IMAGE_SYNTH_ERROR_IMAGE_MASK_MISMATCH;
+      continue;
+    }
+    if (R.parameters) J.p = *R.parameters;
+    else setDefaultParams(&J.p);
+    if ((R.result = prepareImageFormatIndicesFromFormatType(&J.f, R.format))) continue;
+    if (J.p.patchSize > (unsigned)rs::kMaxNeighbors) {
+      R.result = IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+      continue;
+    }
+    J.bpp = countPixelelsPerPixelForFormat(R.format);
+    J.w = R.image->width;
+    J.h = R.image->height;
+    const unsigned w = J.w, h = J.h, d = J.bpp + 1;
+    ImageBuffer* img = R.image;
+    ImageBuffer* cm = R.mask2 ? R.mask2 : R.mask;
+    bool anyTarget = false, anyCorpus = false;
+    for (unsigned y = 0; y < h && !anyTarget; y++)
+      for (unsigned x = 0; x < w && !anyTarget; x++) anyTarget = R.mask->data[y * R.mask->rowBytes + x] != 0;
+    if (!anyTarget) {
+      R.result = IMAGE_SYNTH_ERROR_EMPTY_TARGET;
+      continue;
+    }
+    for (unsigned y = 0; y < h && !anyCorpus; y++)
+      for (unsigned x = 0; x < w && !anyCorpus; x++) {
+        const uint8_t m = cm->data[y * cm->rowBytes + x];
+        const uint8_t cmask = R.mask2 ? m : (uint8_t)~m;
+        anyCorpus = cmask == 0xFF &&
+                    (!J.f.isAlphaSource || img->data[y * img->rowBytes + (size_t)x * J.bpp + J.f.alpha_bip - 1] != 0);
+      }
+    if (!anyCorpus) {
+      R.result = IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
+      continue;
+    }
+    J.imgBytes = img->rowBytes * (h - 1) + (size_t)w * J.bpp;
+    const size_t mBytes = R.mask->rowBytes * (h - 1) + w;
+    J.dImg = ar.alloc<uint8_t>(img->rowBytes * h);
+    uint8_t* dMask = ar.alloc<uint8_t>(R.mask->rowBytes * h);
+    uint8_t* dMask2 = R.mask2 ? ar.alloc<uint8_t>(R.mask2->rowBytes * h) : nullptr;
+    CK(cudaMemcpyAsync(J.dImg, img->data, J.imgBytes, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dMask, R.mask->data, mBytes, cudaMemcpyHostToDevice, s));
+    h2d += J.imgBytes + mBytes;
+    if (R.mask2) {
+      const size_t m2Bytes = R.mask2->rowBytes * (h - 1) + w;
+      CK(cudaMemcpyAsync(dMask2, R.mask2->data, m2Bytes, cudaMemcpyHostToDevice, s));
+      h2d += m2Bytes;
+    }
+    J.dT = ar.alloc<uint8_t>((size_t)w * h * d);
+    uint8_t* dC = ar.alloc<uint8_t>((size_t)w * h * d);
+    CK(rs_adapt(J.dImg, img->rowBytes, dMask, R.mask->rowBytes, dMask2, R.mask2 ? R.mask2->rowBytes : 0, (int)w,
+                (int)h, (int)J.bpp, J.dT, dC, s));
+    const long long maxD2 = wave_radius2((int)w, (int)h);
+    int nWave = 0;
+    const int2* dWave = wave_offsets_device(nWave);
+    const std::vector<int2>& wl = wave_offsets_host();
+    nWave = (int)(std::partition_point(wl.begin(), wl.end(), [&](const int2& o) {
+                    return (long long)o.x * o.x + (long long)o.y * o.y <= maxD2;
+                  }) - wl.begin());
+    const std::vector<int2> noList;
+    J.dp = make_problem(ar, s, J.p, J.f, J.dT, w, h, dC, w, h, nullptr, nullptr, noList, maxD2, h2d, launches, dWave,
+                        nWave);
+    const size_t tn = (size_t)w * h;
+    int* scratch = ar.alloc<int>((size_t)rs_prep_scratch_ints((int)w, (int)h));
+    J.dCounts = ar.alloc<int>(4);
+    J.dTargets = ar.alloc<int2>(tn);
+    J.cpts = ar.alloc<int2>(tn);
+    CK(rs_prep_target(J.dT, (int)w, (int)h, J.f.total_bpp, J.f.alpha_bip, J.f.isAlphaTarget ? 1 : 0,
+                      J.p.matchContextType ? 1 : 0, J.dp.pb.has, J.dp.pb.src, scratch, J.dTargets, J.dCounts, s));
+    CK(rs_prep_corpus(dC, (int)w, (int)h, J.f.total_bpp, J.f.alpha_bip, J.f.isAlphaSource ? 1 : 0, scratch, J.cpts,
+                      J.dCounts + 2, s));
+    launches += 8;
+  }
+  // 2. target and corpus counts of every request: one synchronisation
+  std::vector<int> counts(4 * jobs.size(), 0);
+  for (size_t i = 0; i < jobs.size(); i++)
+    if (jobs[i].dCounts) CK(cudaMemcpyAsync(&counts[4 * i], jobs[i].dCounts, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  rs::Counters* ctrs = ar.alloc<rs::Counters>(jobs.size());
+  CK(cudaMemsetAsync(ctrs, 0, jobs.size() * sizeof(rs::Counters), s));
+  for (size_t i = 0; i < jobs.size(); i++) {
+    BatchJob& J = jobs[i];
+    if (!J.dCounts) continue;
+    J.ntargets = (unsigned)counts[4 * i];
+    J.noContext = counts[4 * i + 1] == 0;
+    const int ncorpus = counts[4 * i + 2];
+    if (!J.ntargets) {   // lib/engine.c:605-627
+      J.req->result = IMAGE_SYNTH_ERROR_EMPTY_TARGET;
+      continue;
+    }
+    if (!ncorpus) {
+      J.req->result = IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
+      continue;
+    }
+    rs::Problem& pb = J.dp.pb;
+    pb.cpts = J.cpts;
+    pb.ncorpus = ncorpus;
+    pb.fullCorpus = (size_t)ncorpus == (size_t)J.w * J.h ? 1 : 0;
+    pass_schedule(J.ntargets, J.ends, J.estimated);
+    J.k = opt.phaseSide ? (int)opt.phaseSide : phase_side_box(wave_offsets_host(), pb.patchLimit, (int)J.w, (int)J.h);
+    J.tiled = pb.tileH || pb.tileV;
+    const size_t tn = (size_t)J.w * J.h;
+    J.vis = ar.alloc<int>(tn);
+    CK(rs_vis_init(pb.has, (int)tn, J.vis, s));
+    launches++;
+    pb.vis = J.vis;
+    J.cellsW = ((int)J.w + rs::kCell - 1) >> rs::kCellShift;
+    J.cellsH = ((int)J.h + rs::kCell - 1) >> rs::kCellShift;
+    J.cellMin = J.tiled ? nullptr : ar.alloc<int>((size_t)J.cellsW * J.cellsH);
+    J.batchStart = ar.alloc<int>((size_t)kMaxBands * J.k * J.k + 1);
+    J.work = ar.alloc<int>(rs_prep_batches_ints((int)J.ntargets, kMaxBands * J.k * J.k));
+    J.dPass = ar.alloc<int2>(J.ntargets);
+    J.dBandEnds = ar.alloc<int>(kMaxBands);
+    J.dBandPhased = ar.alloc<int>(kMaxBands);
+    rs::WaveArgs& wa = J.wa;
+    wa.pb = pb;
+    wa.trys = J.p.maxProbeCount;
+    wa.seed = opt.seed ? opt.seed : 1198472u;
+    wa.ctr = ctrs + i;
+    wa.abortFlag = st.abortDev;
+    wa.sparseLimit2 = 4LL * pb.patchLimit * (long long)J.ntargets;
+    wa.stageSrc = ar.alloc<int2>(J.ntargets);
+    wa.targets = J.dPass;
+    wa.batchStart = J.batchStart;
+    wa.probeShare = (!rs_wave_corpus_staged(pb, 16) && J.ntargets >= 131072u) ? 1 : 0;
+    J.active = true;
+  }
+  // 3. passes
+  std::vector<rs::Counters> hostCtr(jobs.size());
+  std::vector<int> visited(jobs.size(), 0);
+  rs::WaveArgs* dJobs = ar.alloc<rs::WaveArgs>(jobs.size());
+  int* dPrefix = ar.alloc<int>(jobs.size() + 1);
+  std::vector<rs::WaveArgs> hJobs;
+  for (int pass = 0; pass < rs::kPasses; pass++) {
+    std::vector<size_t> act;
+    for (size_t i = 0; i < jobs.size(); i++)
+      if (jobs[i].active) act.push_back(i);
+    if (act.empty()) break;
+    for (size_t i : act) {
+      BatchJob& J = jobs[i];
+      const int k = J.k;
+      const unsigned end = J.ends[pass];
+      // pass-0 bands grow 2x from 16 (random orders); later passes one band
+      J.bandEnds.clear();
+      if (pass == 0) {
+        double size = opt.firstBatch ? opt.firstBatch : 16u, b = 0;
+        const double growth = (opt.bandGrowth ? opt.bandGrowth : 200u) / 100.0;
+        while (b < end && (int)J.bandEnds.size() < kMaxBands - 1) {
+          b = std::min<double>(end, b + std::max(1.0, size));
+          J.bandEnds.push_back((int)b);
+          size *= growth;
+        }
+        if (J.bandEnds.back() < (int)end) J.bandEnds.push_back((int)end);
+      } else {
+        const unsigned refine = opt.refineBatches ? opt.refineBatches : 1u;
+        for (unsigned r = 1; r <= refine; r++) J.bandEnds.push_back((int)((unsigned long long)end * r / refine));
+      }
+      const int nb = (int)J.bandEnds.size();
+      const std::vector<int> phased(nb, 1);
+      CK(cudaMemcpyAsync(J.dBandEnds, J.bandEnds.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(J.dBandPhased, phased.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
+      h2d += 2 * nb * sizeof(int);
+      CK(rs_prep_batches(J.dTargets, (int)J.ntargets, (int)J.w, (int)end, 1, J.wa.seed ^ 0x5bd1e995u, J.dBandEnds,
+                         J.dBandPhased, nb, k, J.work, J.batchStart, J.dPass, pass == 0 ? J.vis : nullptr, s));
+      launches += 4;
+      J.wa.inPlace = (J.tiled || pass > 0) ? 0 : 1;
+      J.wa.pb.cellMin = nullptr;
+      if (pass == 0 && J.cellMin) {
+        CK(rs_cell_min(J.vis, (int)J.w, (int)J.h, J.cellMin, s));
+        launches++;
+        J.wa.pb.cellMin = J.cellMin;
+        J.wa.pb.cellsW = J.cellsW;
+        J.wa.pb.cellsH = J.cellsH;
+      }
+      J.wa.pass = (unsigned)pass;
+      J.wa.sparse = (pass == 0 && J.noContext && !J.tiled) ? 1 : 0;
+      J.wa.nbatches = nb * k * k;
+    }
+    // requests grouped by pixel layout, one launch per group per step
+    std::map<std::pair<int, int>, std::vector<size_t>> groups;
+    for (size_t i : act) groups[{jobs[i].dp.pb.nc, jobs[i].dp.pb.nm > 0 ? 1 : 0}].push_back(i);
+    for (auto& g : groups) {
+      const std::vector<size_t>& idx = g.second;
+      hJobs.clear();
+      int steps = 0;
+      bool staged = false;
+      for (size_t i : idx) {
+        hJobs.push_back(jobs[i].wa);
+        steps = std::max(steps, jobs[i].wa.nbatches);
+        staged |= !jobs[i].wa.inPlace;
+      }
+      CK(cudaMemcpyAsync(dJobs, hJobs.data(), hJobs.size() * sizeof(rs::WaveArgs), cudaMemcpyHostToDevice, s));
+      h2d += hJobs.size() * sizeof(rs::WaveArgs);
+      const int n = (int)idx.size();
+      for (int b = 0; b < steps; b++) {
+        // grid cap from the expected step size: each request's band spread
+        // over its k * k phases, twice that for the spread
+        long long expect = 4;
+        for (size_t i : idx) {
+          const BatchJob& J = jobs[i];
+          if (b >= J.wa.nbatches) continue;
+          const int band = b / (J.k * J.k);
+          const long long c = J.bandEnds[band] - (band ? J.bandEnds[band - 1] : 0);
+          expect += 2 * ((c + J.k * J.k - 1) / (J.k * J.k));
+        }
+        const int maxCtas = expect < (1 << 20) ? (int)expect : 0;
+        CK(rs_launch_multi_prefix(dJobs, n, b, dPrefix, s));
+        CK(rs_launch_wave_multi(dJobs, n, dPrefix, b, pass == 0 ? b : 0x7ffffffe, g.first.first, g.first.second,
+                                maxCtas, st.abortDev, s));
+        launches += 2;
+        if (staged) {
+          CK(rs_launch_commit_multi(dJobs, n, dPrefix, b, (int)std::min<long long>(1 << 20, expect / 256 + 1), s));
+          launches++;
+        }
+      }
+    }
+    CK(cudaMemcpyAsync(hostCtr.data(), ctrs, jobs.size() * sizeof(rs::Counters), cudaMemcpyDeviceToHost, s));
+    for (size_t i : act)
+      CK(cudaMemcpyAsync(&visited[i], jobs[i].batchStart + jobs[i].wa.nbatches, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(epass, s));
+    wait_stream(st, epass, nullptr);
+    for (size_t i : act) {
+      BatchJob& J = jobs[i];
+      const rs::Counters& c = hostCtr[i];
+      if (c.error) return fail(RESYNTH_ERROR_DEVICE, "wavefront kernel reported error %u", c.error);
+      const unsigned betters = c.betters - J.bettersTotal;
+      J.bettersTotal = c.betters;
+      J.passes = pass + 1;
+      stats.visits += (unsigned)visited[i];
+      if ((float)betters / J.ntargets < 0.1 && pass + 1 >= (int)opt.minPasses) J.active = false;   // lib/refiner.h:111
+    }
+  }
+  // 4. results: colours back into the caller's layout, one copy per request
+  for (BatchJob& J : jobs) {
+    if (!J.dT || J.req->result) continue;
+    CK(rs_launch_unpack_colors(J.dT, (int)J.w, (int)J.h, J.f.total_bpp, J.f.img_match_bpp, J.dp.tpx, s));
+    CK(rs_unadapt(J.dT, (int)J.w, (int)J.h, (int)J.bpp, J.dImg, J.req->image->rowBytes, s));
+    CK(cudaMemcpyAsync(J.req->image->data, J.dImg, J.imgBytes, cudaMemcpyDeviceToHost, s));
+    d2h += J.imgBytes;
+    launches += 2;
+    stats.passes = std::max(stats.passes, J.passes);
+  }
+  CK(cudaEventRecord(e1, s));
+  CK(cudaStreamSynchronize(s));
+  for (size_t i = 0; i < jobs.size(); i++)
+    if (jobs[i].dCounts) {
+      stats.evals += hostCtr[i].evals;
+      stats.terms += hostCtr[i].terms;
+    }
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  stats.deviceMs += ms;
+  stats.launches += launches;
+  stats.h2dBytes += h2d;
+  stats.d2hBytes += d2h;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(epass);
+  return 0;
+}
+
 // engine() core on host pixmaps.
 int run_engine_host(const TImageSynthParameters& p, const TFormatIndices& f, uint8_t* target, unsigned tw,
                     unsigned th, const uint8_t* corpus, unsigned cw, unsigned ch, void (*cb)(int, void*), void* ctx,
@@ -1380,20 +1721,37 @@ RS_EXPORT int imageSynthBatch(TResynthRequest* requests, unsigned int count, uns
   const TResynthOptions opt = options_or_default(options);
   const unsigned workers = std::max(1u, std::min(count, concurrency ? concurrency : 8u));
   std::vector<TResynthStats> per(count);
+  // Wavefront requests with a random order go through the many-request
+  // launches (unless options->separateRequests); the rest through workers.
+  std::vector<TResynthRequest*> multi;
+  std::vector<unsigned> rest;
+  for (unsigned i = 0; i < count; i++) {
+    if (!opt.separateRequests && batch_eligible(requests[i], opt)) multi.push_back(&requests[i]);
+    else rest.push_back(i);
+  }
+  TResynthStats multiStats{};
+  int multiRc = 0;
+  if (!multi.empty()) {
+    multiRc = guarded("imageSynthBatch", [&] { return run_batch_wave(multi, opt, multiStats); });
+    if (multiRc)
+      for (TResynthRequest* r : multi) r->result = multiRc;
+  }
   std::atomic<unsigned> next{0};
   auto work = [&] {
-    for (unsigned i = next++; i < count; i = next++) {
-      TResynthRequest& r = requests[i];
+    for (unsigned j = next++; j < rest.size(); j = next++) {
+      TResynthRequest& r = requests[rest[j]];
       r.result = imageSynthEx(r.image, r.mask, r.mask2, r.format, r.parameters, nullptr, nullptr, nullptr, &opt,
-                              &per[i]);
+                              &per[rest[j]]);
     }
   };
   std::vector<std::thread> pool;
-  for (unsigned w = 1; w < workers; w++) pool.emplace_back(work);
-  work();
+  if (!rest.empty()) {
+    for (unsigned w = 1; w < std::min<unsigned>(workers, (unsigned)rest.size()); w++) pool.emplace_back(work);
+    work();
+  }
   for (auto& t : pool) t.join();
   int rc = 0;
-  TResynthStats total{};
+  TResynthStats total = multiStats;
   for (unsigned i = 0; i < count; i++) {
     if (!rc && requests[i].result) rc = requests[i].result;
     total.visits += per[i].visits;

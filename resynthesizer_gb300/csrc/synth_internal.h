@@ -93,6 +93,7 @@ struct WaveArgs {
   int nprop;                     // how many of each target's 16 are scored
   int propBatch0;                // the band's first batch: props index = t - batchStart[propBatch0]
   int probeShare;                // random probes keyed by (batch, slot / 16) instead of the pixel
+  int nbatches;                  // many-request steps: batches of this pass (0 = inactive)
 };
 
 // Frozen-state scoring and energy.
@@ -122,6 +123,11 @@ cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream
 cudaError_t rs_launch_wave(const rs::WaveArgs& a, int warpsPerBlock, int maxCtas, cudaStream_t s);
 cudaError_t rs_launch_commit(const rs::WaveArgs& a, int maxCtas, cudaStream_t s);
 int rs_wave_corpus_staged(const rs::Problem& pb, int warps);
+cudaError_t rs_launch_wave_multi(const rs::WaveArgs* jobs, int nreq, const int* prefix, int step, int visCur, int nc,
+                                 int map, int maxCtas, const volatile int* abortFlag, cudaStream_t s);
+cudaError_t rs_launch_multi_prefix(const rs::WaveArgs* jobs, int nreq, int step, int* prefix, cudaStream_t s);
+cudaError_t rs_launch_commit_multi(const rs::WaveArgs* jobs, int nreq, const int* prefix, int step, int maxCtas,
+                                   cudaStream_t s);
 cudaError_t rs_launch_frozen(const rs::ScoreArgs& a, cudaStream_t s);
 cudaError_t rs_launch_energy(const rs::ScoreArgs& a, cudaStream_t s);
 cudaError_t rs_prep_target(const uint8_t* raw, int w, int h, int bpp, int alpha, int hasAlpha, int useContext,

@@ -763,23 +763,183 @@ struct WaveSmem {
   static constexpr int kHead = 2 * 256 * 4 + 16;   // half tables + two mbarriers
 };
 
-// One wavefront batch: a warp per target.  Candidates are the deduplicated
+// Shared memory and team layout of one CTA of the wavefront kernels: warps
+// form teams of G (a power of two); a team's patch and candidate list live in
+// its first warp's region.
+struct WaveTeam {
+  int G, team, tw, lead, lane, warp;
+  unsigned char* regions;        // per-warp regions (WaveSmem::kPerWarp each)
+  unsigned long long* sKey;      // [16]
+  int *sN, *sNp, *sFast, *sGather;   // [16] each
+  __device__ __forceinline__ void sync() const {
+    if (G == 1) __syncwarp();
+    else asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(G * 32) : "memory");
+  }
+  __device__ __forceinline__ unsigned char* region(int w) const { return regions + w * WaveSmem::kPerWarp; }
+};
+
+// One target of a wavefront batch (slot `slot` of the batch starting at b0 in
+// a.targets), synthesized by one team.  Candidates are the deduplicated
 // in-corpus continuations of the patch's sources, then (with a proposal
 // network) the network's proposals, then `trys` counter-based random probes;
 // the best (first strict minimum) different source is stored in place, or
-// staged for k_commit when the target wraps.
+// staged for k_commit.  Returns 1 if the target's source changed (in place).
+template <int NC, bool MAP>
+__device__ __forceinline__ unsigned wave_target(const WaveArgs& a, const Problem& pb, const CorpusView& cv,
+                                                const uint32_t* ct, const uint32_t* mt, int batch, int visCur,
+                                                int b0, int slot, bool sparse, const WaveTeam& T, unsigned& terms,
+                                                unsigned& evals) {
+  const int G = T.G, tw = T.tw, lead = T.lead, lane = T.lane, warp = T.warp;
+  unsigned char* wbase = T.region(lead);
+  Patch& P = *reinterpret_cast<Patch*>(wbase);
+  unsigned long long* topk = reinterpret_cast<unsigned long long*>(wbase + sizeof(Patch));
+  int2* prop = reinterpret_cast<int2*>(topk);
+  const int t = b0 + slot;
+  const int2 pos = a.targets[t];
+  const int pi = pos.y * pb.tw + pos.x;
+  // The patch.  While the valued pixels are a short list, every warp of the
+  // team collects the nearest keys of its share of the list and the lead
+  // merges them; otherwise the lead walks the offset list, falling back to
+  // the cell grid when the nearest values lie beyond the walk's reach.
+  int nPatch = 0;
+  if (sparse) {
+    unsigned long long* mine = reinterpret_cast<unsigned long long*>(T.region(warp) + sizeof(Patch));
+    int cnt = 0;
+    unsigned long long thr = ~0ull;
+    sparse_keys(pb, pos.x, pos.y, mine, cnt, thr, a.targets, b0, lane, tw, G);
+    if (G > 1) {
+      if (lane == 0) T.sGather[warp] = cnt;
+      T.sync();
+      if (tw == 0)
+        for (int w = 1; w < G; w++)
+          merge_keys(mine, cnt, thr, pb.patchLimit - 1,
+                     reinterpret_cast<const unsigned long long*>(T.region(lead + w) + sizeof(Patch)),
+                     T.sGather[lead + w], lane);
+    }
+    if (tw == 0) nPatch = patch_from_keys(pb, pos.x, pos.y, P, mine, cnt, lane);
+  } else if (tw == 0) {
+    nPatch = build_patch_warp(pb, pos.x, pos.y, P, lane, visCur, pb.cellMin ? kScanCap : INT_MAX);
+    if (pb.cellMin && nPatch < pb.patchLimit && kScanCap < pb.noffs)
+      nPatch = build_patch_grid(pb, pos.x, pos.y, P, topk, lane, visCur);
+  }
+  if (tw == 0) {
+    const int n = nPatch;
+    // linear offsets into the padded corpus; the fast path needs all within kPad
+    int far = 0;
+    for (int i = lane; i < n; i += 32) {
+      const int dx = off_dx(P.off[i]), dy = off_dy(P.off[i]);
+      P.doff[i] = dy * pb.padW + dx;
+      far |= (abs(dx) > kPad) | (abs(dy) > kPad);
+    }
+    far = __any_sync(kFull, far);
+    // continuation candidates, deduplicated, in neighbour order
+    int np = 0;
+    for (int r = 0; r < n; r += 32) {
+      const int k = r + lane;
+      bool valid = false;
+      int2 c = make_int2(0, 0);
+      if (k < n && P.src[k].x >= 0) {
+        c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
+        valid = corpus_ok(pb, cv, c);
+      }
+      const unsigned long long key =
+          valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
+      const unsigned peers = __match_any_sync(kFull, key);
+      bool keep = valid && (peers & lanemask_lt()) == 0u;
+      for (int e = 0; e < np && keep; e++)
+        if (prop[e].x == c.x && prop[e].y == c.y) keep = false;
+      const unsigned km = __ballot_sync(kFull, keep);
+      if (keep) prop[np + __popc(km & lanemask_lt())] = c;
+      np += __popc(km);
+      __syncwarp();
+    }
+    if (lane == 0) {
+      T.sN[lead] = n;
+      T.sNp[lead] = np;
+      T.sFast[lead] = !far;
+    }
+  }
+  T.sync();
+  const int n = T.sN[lead], np = T.sNp[lead];
+  const bool fast = T.sFast[lead] != 0;
+  // Candidates: continuations, then the network's proposals (an invalid
+  // one is replaced by an extra probe), then the random probes.
+  const int nprop = a.props ? a.nprop : 0;
+  const int ncand = np + nprop + (int)a.trys;
+  // Probe keys: per target pixel, or shared by 16 consecutive slots of the
+  // batch (neighbours in the target list, which the batches keep in order):
+  // the warps of a CTA then read the same random corpus windows, which stay
+  // in L1/L2 when the corpus itself is too large to.
+  const uint32_t pbase = a.probeShare
+                             ? probe_base(a.seed ^ 0x6A09E667u, a.pass, (uint32_t)batch * 0x01000193u + ((uint32_t)slot >> 4))
+                             : probe_base(a.seed, a.pass, (uint32_t)pi);
+  const int2* myProps = nprop ? a.props + (size_t)(t - a.batchStart[a.propBatch0]) * 16 : nullptr;
+  auto cand = [&](int k) -> int2 {
+    if (k < np) return prop[k];
+    if (k < np + nprop) {
+      const int2 c = myProps[k - np];
+      return corpus_ok(pb, cv, c) ? c : probe_point(pb, pbase, a.trys + (uint32_t)(k - np));
+    }
+    return probe_point(pb, pbase, (uint32_t)(k - np - nprop));
+  };
+  // Warp tw of the team scores candidates tw, tw + G, tw + 2G, ...
+  const int nloc = ncand > tw ? (ncand - tw + G - 1) / G : 0;
+  uint32_t bv;
+  int bi;
+  auto get = [&](int j) { return cand(tw + j * G); };
+  if (fast)
+    score_warp<NC, MAP, true>(pb, cv, ct, mt, P, n, nloc, get, lane, bv, bi, terms, evals);
+  else
+    score_warp<NC, MAP, false>(pb, cv, ct, mt, P, n, nloc, get, lane, bv, bi, terms, evals);
+  if (lane == 0) T.sKey[warp] = bi == INT_MAX ? ~0ull : ((unsigned long long)bv << 32) | (unsigned)(tw + bi * G);
+  T.sync();
+  unsigned better = 0;
+  if (tw == 0 && lane == 0) {
+    unsigned long long best = ~0ull;
+    for (int w = 0; w < G; w++) best = min(best, T.sKey[lead + w]);
+    int2 out = make_int2(-2, -2);
+    if (best != ~0ull) {
+      const int k = (int)(best & 0xffffffffu);
+      const int2 pt = cand(k);
+      const int2 cur = pb.src[pi];
+      if (cur.x != pt.x || cur.y != pt.y) out = pt;
+    }
+    if (a.inPlace) {
+      // No target of this batch reads another's state (visit stamps, colour
+      // phases), so the store (setColor + setSourceOf) happens right here.
+      if (out.x != -2) {
+        const uint32_t c = pb.cpx[out.y * pb.cw + out.x];
+        pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (c & 0xFFFFFF00u);
+        pb.src[pi] = out;
+        better = 1;
+      }
+    } else {
+      a.stageSrc[slot] = out;
+    }
+  }
+  T.sync();
+  return better;
+}
+
+// Team size: when the step has fewer targets than the grid has warps, G warps
+// (a power of two, at most the CTA) share one target's candidates.  The result
+// does not depend on G: every team reduces to the same (sum, candidate index)
+// minimum.
+__device__ __forceinline__ int team_size(int nslots) {
+  const int wpb = blockDim.x >> 5;
+  int G = 1;
+  while (G < wpb && (long long)nslots * (G * 2) <= (long long)gridDim.x * wpb) G *= 2;
+  return G;
+}
+
+// One wavefront batch of one problem: a team of warps per target.
 template <int NC, bool MAP, bool SMEMC>
 __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int b0 = a.batchStart[a.batch], b1 = a.batchStart[a.batch + 1];
   const int nslots = b1 - b0;
-  // Team size: when the batch has fewer targets than the grid has warps, G
-  // warps (a power of two, at most the CTA) share one target's candidates.
-  // The result does not depend on G: every team reduces to the same
-  // (sum, candidate index) minimum.
   const int wpb = blockDim.x >> 5;
-  int G = 1;
-  while (G < wpb && (long long)nslots * (G * 2) <= (long long)gridDim.x * wpb) G *= 2;
+  const int G = team_size(nslots);
   const int teamsPerBlock = wpb / G;
   // CTAs beyond this batch's size leave before staging anything.
   if ((int)(blockIdx.x * teamsPerBlock) >= nslots) return;
@@ -815,148 +975,20 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   if (threadIdx.x == 0) s_abort = *a.abortFlag;
   __syncthreads();
   if (s_abort) return;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int team = warp / G, tw = warp % G, lead = team * G;
-  // The team's patch and candidate list live in its first warp's region.
-  unsigned char* wbase = p + lead * WaveSmem::kPerWarp;
-  Patch& P = *reinterpret_cast<Patch*>(wbase);
-  unsigned long long* topk = reinterpret_cast<unsigned long long*>(wbase + sizeof(Patch));
-  int2* prop = reinterpret_cast<int2*>(topk);
   __shared__ unsigned long long s_key[16];
   __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16];
   __shared__ unsigned s_better;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int team = warp / G;
+  const WaveTeam T{G, team, warp % G, team * G, lane, warp, p, s_key, s_n, s_np, s_fast, s_gather};
   if (threadIdx.x == 0) s_better = 0;
   __syncthreads();
-  auto team_sync = [&]() {
-    if (G == 1) __syncwarp();
-    else asm volatile("bar.sync %0, %1;" ::"r"(1 + team), "r"(G * 32) : "memory");
-  };
   const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
   unsigned terms = 0, evals = 0;
   for (int slot = blockIdx.x * teamsPerBlock + team; slot < nslots; slot += gridDim.x * teamsPerBlock) {
-    const int t = b0 + slot;
-    const int2 pos = a.targets[t];
-    const int pi = pos.y * pb.tw + pos.x;
-    // The patch.  While the valued pixels are a short list, every warp of the
-    // team collects the nearest keys of its share of the list and the lead
-    // merges them; otherwise the lead walks the offset list, falling back to
-    // the cell grid when the nearest values lie beyond the walk's reach.
-    int nPatch = 0;
-    if (sparse) {
-      unsigned long long* mine = reinterpret_cast<unsigned long long*>(p + warp * WaveSmem::kPerWarp + sizeof(Patch));
-      int cnt = 0;
-      unsigned long long thr = ~0ull;
-      sparse_keys(pb, pos.x, pos.y, mine, cnt, thr, a.targets, b0, lane, tw, G);
-      if (G > 1) {
-        if (lane == 0) s_gather[warp] = cnt;
-        team_sync();
-        if (tw == 0)
-          for (int w = 1; w < G; w++)
-            merge_keys(mine, cnt, thr, pb.patchLimit - 1,
-                       reinterpret_cast<const unsigned long long*>(p + (lead + w) * WaveSmem::kPerWarp + sizeof(Patch)),
-                       s_gather[lead + w], lane);
-      }
-      if (tw == 0) nPatch = patch_from_keys(pb, pos.x, pos.y, P, mine, cnt, lane);
-    } else if (tw == 0) {
-      nPatch = build_patch_warp(pb, pos.x, pos.y, P, lane, a.visCur, pb.cellMin ? kScanCap : INT_MAX);
-      if (pb.cellMin && nPatch < pb.patchLimit && kScanCap < pb.noffs)
-        nPatch = build_patch_grid(pb, pos.x, pos.y, P, topk, lane, a.visCur);
-    }
-    if (tw == 0) {
-      const int n = nPatch;
-      // linear offsets into the padded corpus; the fast path needs all within kPad
-      int far = 0;
-      for (int i = lane; i < n; i += 32) {
-        const int dx = off_dx(P.off[i]), dy = off_dy(P.off[i]);
-        P.doff[i] = dy * pb.padW + dx;
-        far |= (abs(dx) > kPad) | (abs(dy) > kPad);
-      }
-      far = __any_sync(kFull, far);
-      // continuation candidates, deduplicated, in neighbour order
-      int np = 0;
-      for (int r = 0; r < n; r += 32) {
-        const int k = r + lane;
-        bool valid = false;
-        int2 c = make_int2(0, 0);
-        if (k < n && P.src[k].x >= 0) {
-          c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
-          valid = corpus_ok(pb, cv, c);
-        }
-        const unsigned long long key =
-            valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
-        const unsigned peers = __match_any_sync(kFull, key);
-        bool keep = valid && (peers & lanemask_lt()) == 0u;
-        for (int e = 0; e < np && keep; e++)
-          if (prop[e].x == c.x && prop[e].y == c.y) keep = false;
-        const unsigned km = __ballot_sync(kFull, keep);
-        if (keep) prop[np + __popc(km & lanemask_lt())] = c;
-        np += __popc(km);
-        __syncwarp();
-      }
-      if (lane == 0) {
-        s_n[lead] = n;
-        s_np[lead] = np;
-        s_fast[lead] = !far;
-      }
-    }
-    team_sync();
-    const int n = s_n[lead], np = s_np[lead];
-    const bool fast = s_fast[lead] != 0;
-    // Candidates: continuations, then the network's proposals (an invalid
-    // one is replaced by an extra probe), then the random probes.
-    const int nprop = a.props ? a.nprop : 0;
-    const int ncand = np + nprop + (int)a.trys;
-    // Probe keys: per target pixel, or shared by 16 consecutive slots of the
-    // batch (neighbours in the target list, which the batches keep in order):
-    // the warps of a CTA then read the same random corpus windows, which stay
-    // in L1/L2 when the corpus itself is too large to.
-    const uint32_t pbase = a.probeShare
-                               ? probe_base(a.seed ^ 0x6A09E667u, a.pass, (uint32_t)a.batch * 0x01000193u + ((uint32_t)slot >> 4))
-                               : probe_base(a.seed, a.pass, (uint32_t)pi);
-    const int2* myProps = nprop ? a.props + (size_t)(t - a.batchStart[a.propBatch0]) * 16 : nullptr;
-    auto cand = [&](int k) -> int2 {
-      if (k < np) return prop[k];
-      if (k < np + nprop) {
-        const int2 c = myProps[k - np];
-        return corpus_ok(pb, cv, c) ? c : probe_point(pb, pbase, a.trys + (uint32_t)(k - np));
-      }
-      return probe_point(pb, pbase, (uint32_t)(k - np - nprop));
-    };
-    // Warp tw of the team scores candidates tw, tw + G, tw + 2G, ...
-    const int nloc = ncand > tw ? (ncand - tw + G - 1) / G : 0;
-    uint32_t bv;
-    int bi;
-    auto get = [&](int j) { return cand(tw + j * G); };
-    if (fast)
-      score_warp<NC, MAP, true>(pb, cv, ct, mt, P, n, nloc, get, lane, bv, bi, terms, evals);
-    else
-      score_warp<NC, MAP, false>(pb, cv, ct, mt, P, n, nloc, get, lane, bv, bi, terms, evals);
-    if (lane == 0) s_key[warp] = bi == INT_MAX ? ~0ull : ((unsigned long long)bv << 32) | (unsigned)(tw + bi * G);
-    team_sync();
-    if (tw == 0 && lane == 0) {
-      unsigned long long best = ~0ull;
-      for (int w = 0; w < G; w++) best = min(best, s_key[lead + w]);
-      int2 out = make_int2(-2, -2);
-      if (best != ~0ull) {
-        const int k = (int)(best & 0xffffffffu);
-        const int2 pt = cand(k);
-        const int2 cur = pb.src[pi];
-        if (cur.x != pt.x || cur.y != pt.y) out = pt;
-      }
-      if (a.inPlace) {
-        // No target of this batch reads another's state (visit stamps, colour
-        // phases), so the store (setColor + setSourceOf) happens right here.
-        if (out.x != -2) {
-          const uint32_t c = pb.cpx[out.y * pb.cw + out.x];
-          pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (c & 0xFFFFFF00u);
-          pb.src[pi] = out;
-          atomicAdd(&s_better, 1u);
-        }
-      } else {
-        a.stageSrc[slot] = out;
-      }
-    }
-    team_sync();
+    const unsigned better =
+        wave_target<NC, MAP>(a, pb, cv, ct, mt, a.batch, a.visCur, b0, slot, sparse, T, terms, evals);
+    if (better) atomicAdd(&s_better, 1u);
   }
   __syncthreads();
   if (threadIdx.x == 0 && s_better) atomicAdd(&a.ctr->betters, s_better);
@@ -964,6 +996,116 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   if (lane == 0) {
     atomicAdd(&a.ctr->terms, tv);
     atomicAdd(&a.ctr->evals, ev);
+  }
+}
+
+// The request of global slot gs: prefix[r] <= gs < prefix[r + 1].
+__device__ __forceinline__ int multi_request(const int* prefix, int nreq, int gs) {
+  int lo = 0, hi = nreq - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (prefix[mid] <= gs) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Step `step` of a pass for many problems at once: batch `step` of every
+// request with that many batches, the requests' slots concatenated through
+// `prefix` (exclusive, prefix[nreq] = total).  Corpora and tables are read
+// from global memory; per-request counters take the sums.
+template <int NC, bool MAP>
+__global__ void __launch_bounds__(512, 2) k_wave_multi(const WaveArgs* jobs, int nreq, const int* prefix, int step,
+                                                       int visCur, const volatile int* abortFlag) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int total = prefix[nreq];
+  const int wpb = blockDim.x >> 5;
+  const int G = team_size(total);
+  const int teamsPerBlock = wpb / G;
+  if ((int)(blockIdx.x * teamsPerBlock) >= total) return;
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = *abortFlag;
+  __shared__ unsigned long long s_key[16];
+  __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16];
+  __syncthreads();
+  if (s_abort) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int team = warp / G;
+  const WaveTeam T{G, team, warp % G, team * G, lane, warp, smem + WaveSmem::kHead, s_key, s_n, s_np, s_fast,
+                   s_gather};
+  for (int gs = blockIdx.x * teamsPerBlock + team; gs < total; gs += gridDim.x * teamsPerBlock) {
+    const int r = multi_request(prefix, nreq, gs);
+    const WaveArgs& a = jobs[r];
+    const Problem& pb = a.pb;
+    const CorpusView cv{pb.cpxPad, pb.cmapPad, pb.padW, kPad * pb.padW + kPad};
+    const int b0 = a.batchStart[step];
+    const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
+    unsigned terms = 0, evals = 0;
+    const unsigned better = wave_target<NC, MAP>(a, pb, cv, pb.ctab + 256, pb.mtab + 256, step, visCur, b0,
+                                                 gs - prefix[r], sparse, T, terms, evals);
+    if (better) atomicAdd(&a.ctr->betters, 1u);
+    const unsigned long long tv = warp_sum_u64(terms), ev = warp_sum_u64(evals);
+    if (lane == 0) {
+      atomicAdd(&a.ctr->terms, tv);
+      atomicAdd(&a.ctr->evals, ev);
+    }
+  }
+}
+
+// Slot counts of step `step` for every request (0 past its last batch or when
+// inactive) and their exclusive prefix; one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) k_multi_prefix(const WaveArgs* jobs, int nreq, int step, int* prefix) {
+  __shared__ int warpSums[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < nreq; base += 1024) {
+    const int r = base + threadIdx.x;
+    int v = 0;
+    if (r < nreq && step < jobs[r].nbatches) v = jobs[r].batchStart[step + 1] - jobs[r].batchStart[step];
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = warpSums[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warpSums[lane] = w;
+    }
+    __syncthreads();
+    if (r < nreq) prefix[r] = carry + (warp ? warpSums[warp - 1] : 0) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warpSums[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) prefix[nreq] = carry;
+}
+
+// Staged results of step `step` for many problems.
+__global__ void k_commit_multi(const WaveArgs* jobs, int nreq, const int* prefix, int step) {
+  const int total = prefix[nreq];
+  for (int gs = blockIdx.x * blockDim.x + threadIdx.x; gs < total; gs += gridDim.x * blockDim.x) {
+    const int r = multi_request(prefix, nreq, gs);
+    const WaveArgs& a = jobs[r];
+    if (a.inPlace) continue;
+    const Problem& pb = a.pb;
+    const int slot = gs - prefix[r];
+    const int2 pos = a.targets[a.batchStart[step] + slot];
+    const int pi = pos.y * pb.tw + pos.x;
+    const int2 s = a.stageSrc[slot];
+    if (s.x != -2) {
+      const uint32_t c = pb.cpx[s.y * pb.cw + s.x];
+      pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (c & 0xFFFFFF00u);
+      pb.src[pi] = s;
+      atomicAdd(&a.ctr->betters, 1u);
+    }
   }
 }
 
@@ -1185,6 +1327,53 @@ extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, int maxCtas,
     RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_t<NC, MAP, false>(a, warps, maxCtas, smem, s)));
   }
   return e;
+}
+
+namespace {
+template <int NC, bool MAP>
+cudaError_t launch_wave_multi_t(const WaveArgs* jobs, int nreq, const int* prefix, int step, int visCur, int maxCtas,
+                                const volatile int* abortFlag, cudaStream_t s) {
+  auto kern = k_wave_multi<NC, MAP>;
+  constexpr int warps = 16;
+  const size_t smem = WaveSmem::kHead + (size_t)warps * WaveSmem::kPerWarp;
+  static std::mutex mu;
+  static int perSm = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!perSm) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  if (perSm < 1) return cudaErrorInvalidConfiguration;
+  int grid = sm_count() * perSm;
+  if (maxCtas > 0) grid = std::min(grid, maxCtas);
+  kern<<<grid, warps * 32, smem, s>>>(jobs, nreq, prefix, step, visCur, abortFlag);
+  return cudaGetLastError();
+}
+}  // namespace
+
+// Step `step` of many problems of one pixel layout (nc colour channels, maps or not).
+extern "C" cudaError_t rs_launch_wave_multi(const WaveArgs* jobs, int nreq, const int* prefix, int step, int visCur,
+                                            int nc, int map, int maxCtas, const volatile int* abortFlag,
+                                            cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  RS_DISPATCH(nc, map != 0, (e = launch_wave_multi_t<NC, MAP>(jobs, nreq, prefix, step, visCur, maxCtas, abortFlag, s)));
+  return e;
+}
+
+extern "C" cudaError_t rs_launch_multi_prefix(const WaveArgs* jobs, int nreq, int step, int* prefix, cudaStream_t s) {
+  k_multi_prefix<<<1, 1024, 0, s>>>(jobs, nreq, step, prefix);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_launch_commit_multi(const WaveArgs* jobs, int nreq, const int* prefix, int step, int maxCtas,
+                                              cudaStream_t s) {
+  int grid = sm_count() * 2;
+  if (maxCtas > 0) grid = std::min(grid, maxCtas);
+  k_commit_multi<<<grid, 256, 0, s>>>(jobs, nreq, prefix, step);
+  return cudaGetLastError();
 }
 
 extern "C" int rs_wave_corpus_staged(const Problem& pb, int warps) {
