@@ -219,7 +219,7 @@ def run_quality(args):
 
 
 def run_batch(args):
-    """Batched heal requests (SURVEY c3): independent heals of mixed sizes,
+    """Batched heal requests: independent heals of mixed sizes,
     layouts, holes and patch sizes through imageSynthBatch, end to end with
     host buffers.  value = all requests' target pixels / wall time."""
     import numpy as np

@@ -314,7 +314,7 @@ int resynthTcGemm(const float *A, const float *B, int M, int N, int K, float *D)
  * mode (TResynthOptions.net) they join each visit's candidates next to the
  * neighbours' continuations and the random probes (lib/synthesize.h:536-604)
  * and are scored by the same exact metric, so the plain search stays both
- * fallback and judge.
+ * fallback and arbiter.
  *
  * Context: 11 x 11 pixels x 16 bf16 channels, row-major (y, x, channel),
  * centred on the target.  Channels 0-2 colour (grey repeated) as v/255 - 0.5,

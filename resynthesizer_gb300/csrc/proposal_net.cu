@@ -4,7 +4,7 @@
 // sources for the synthesis search, whose only other candidates are the
 // neighbours' continuations and uniform random draws (lib/synthesize.h:
 // 536-604).  Every proposal is scored by the exact integer patch metric, so
-// the plain search stays both fallback and judge.
+// the plain search stays both the fallback and the arbiter.
 //
 // Network: an 11 x 11 x 16 context (colour, has-value, map) around a target
 // pixel; four 3x3 convolutions of 32 channels with ReLU (11 -> 9 -> 7 -> 5 ->
