@@ -107,6 +107,24 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(value: float, device=None) -> float:
+    """The largest value over the ranks of the default process group (the
+    value itself without one): replicas report the slowest rank's time."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, steps: int, units_per_step: float, max_ms: float) -> float:
+    """Whole-job throughput of `world` replicas that each processed `steps`
+    steps of `units_per_step` units, timed by the slowest one."""
+    return world * steps * units_per_step / (max_ms / 1000.0)
+
+
 def cpu_sample(threads: int, side: int = SAMPLE_SIDE):
     """The CPU engine on a side x side sample of the workload: the reference
     built from its own sources where present, else the oracle port."""
@@ -451,13 +469,10 @@ def main():
             ms.append(e0.elapsed_time(e1))
             evals += st["evals"]
             launches += st["launches"]
-    total_ms = sum(ms)
+    total_ms = max_over_ranks(sum(ms), dev)
     if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
-    value = world * args.steps * target_px / (total_ms / 1000.0)
+    value = replica_throughput(world, args.steps, target_px, total_ms)
     evals_per_s = world * evals / (total_ms / 1000.0)
 
     # end to end through the reference-facing call with host buffers
