@@ -152,13 +152,16 @@ typedef struct {
   int profile;                /* time each synthesis-kernel launch with CUDA events (stats.waveMs) */
   unsigned int phaseSide;     /* wavefront: k of the k x k colour phases (0 = from the patch radius, 1 = none) */
   unsigned int bandGrowth;    /* wavefront: pass-0 band growth in percent for random orders (0 = 200) */
-  unsigned int minPasses;     /* wavefront: run at least this many passes (0 = the reference's stop rule only) */
+  unsigned int minPasses;     /* wavefront: run at least this many passes; 0 = default (3 for texture synthesis
+                                 without context or map channels, else the reference's stop rule alone), 1 = the
+                                 reference's stop rule alone */
   TResynthNet *net;           /* wavefront: score this network's proposals at every visit (NULL = none) */
   unsigned int proposals;     /* wavefront: how many of the network's 16 offsets are scored (0 = none) */
   TResynthPairs *dumpPairs;   /* wavefront: append (context, final source) training pairs at the end */
   unsigned int dumpStride;    /* every dumpStride-th target of the visit order gives a pair (0 = 16) */
   int graphs;                 /* wavefront: launch each pass as one captured CUDA graph */
   int separateRequests;       /* imageSynthBatch: one stream per request instead of the many-request launches */
+  unsigned int bandGrowthLarge; /* wavefront: growth in percent of pass-0 bands of at least 1/64 of the pass (0 = default) */
 } TResynthOptions;
 
 typedef struct {

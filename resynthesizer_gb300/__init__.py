@@ -60,7 +60,7 @@ class Options(C.Structure):
                 ("warpsPerBlock", C.c_uint), ("recordState", C.c_int), ("profile", C.c_int),
                 ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint),
                 ("net", C.c_void_p), ("proposals", C.c_uint), ("dumpPairs", C.c_void_p), ("dumpStride", C.c_uint),
-                ("graphs", C.c_int), ("separateRequests", C.c_int)]
+                ("graphs", C.c_int), ("separateRequests", C.c_int), ("bandGrowthLarge", C.c_uint)]
 
 
 class TrainOptions(C.Structure):
@@ -182,7 +182,7 @@ def format_indices(colors, mapColors=0, alphaTarget=0, alphaSource=0, isMap=0) -
 
 def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, recordState=0,
             profile=0, phaseSide=0, bandGrowth=0, minPasses=0, net=None, proposals=0, dump=None,
-            dumpStride=0, graphs=0, separateRequests=0) -> Options:
+            dumpStride=0, graphs=0, separateRequests=0, bandGrowthLarge=0) -> Options:
     o = Options()
     lib().resynthDefaultOptions(C.byref(o))
     if mode is not None:
@@ -196,6 +196,7 @@ def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, r
     o.dumpStride = dumpStride
     o.graphs = graphs
     o.separateRequests = separateRequests
+    o.bandGrowthLarge = bandGrowthLarge
     return o
 
 

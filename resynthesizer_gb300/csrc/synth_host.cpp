@@ -567,6 +567,23 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
 
 // Radius (squared) of the offset list used by the wavefront mode: enough for
 // any dense patch; sparse early batches look this far for context.
+// Growth of the large pass-0 bands (percent): once a band holds 1/64 of the
+// pass, bands grow more slowly, so that fewer targets share a batch when the
+// neighbourhoods are dense (energy); the small bands before are latency-bound
+// and keep doubling.
+constexpr unsigned kDefaultGrowthLarge = 200;
+
+// Passes the wavefront runs at least.  Texture synthesis from nothing (no
+// context, no map channels) ends its second pass with a patch energy about
+// 1.5 % above the reference's threaded engine (the targets of a batch do not
+// see each other); a third pass brings it under 1 % (render1024: 1.0148 ->
+// 1.0066 of the threaded mean, 4 seeds against 8 runs).  Heals and map-guided
+// runs meet the energy of the reference with its own stop rule.
+int wave_min_passes(const TResynthOptions& opt, bool noContext, int mapChannels) {
+  if (opt.minPasses) return (int)opt.minPasses;
+  return noContext && mapChannels == 0 ? 3 : 0;
+}
+
 unsigned ilog2(uint64_t v) {
   unsigned r = 0;
   while (v >>= 1) r++;
@@ -797,6 +814,8 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     const unsigned first = opt.firstBatch ? opt.firstBatch : (randomOrder ? 16u : 1024u);
     const unsigned refine = opt.refineBatches ? opt.refineBatches : 1u;
     const double growth = (opt.bandGrowth ? opt.bandGrowth : 200u) / 100.0;
+    const double growthLarge = (opt.bandGrowthLarge ? opt.bandGrowthLarge : kDefaultGrowthLarge) / 100.0;
+    const int minPasses = wave_min_passes(opt, noContext, dp.pb.nm);
     const int k = opt.phaseSide ? (int)opt.phaseSide : phase_side_box(wave_offsets_host(), dp.pb.patchLimit, mw, mh);
     constexpr int kMaxBands = 64;
     // While no pixel outside the current pass has a value, a batch's patches
@@ -860,7 +879,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
         while (b < end && (int)bandEnds.size() < kMaxBands - 1) {
           b = std::min<double>(end, b + std::max(1.0, size));
           bandEnds.push_back((int)b);
-          if (randomOrder) size *= growth;
+          if (randomOrder) size *= size * 64 < end ? growth : growthLarge;
         }
         if (bandEnds.back() < (int)end) bandEnds.push_back((int)end);
       } else {
@@ -978,7 +997,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       stats.passLength[pass] = visited;
       stats.betters[pass] = betters;
       if (*cancel || *st.abortHost) break;
-      if ((float)betters / ntargets < 0.1 && pass + 1 >= (int)opt.minPasses) break;   // lib/refiner.h:111
+      if ((float)betters / ntargets < 0.1 && pass + 1 >= minPasses) break;   // lib/refiner.h:111
     }
     stats.visits = 0;
     for (unsigned i = 0; i < stats.passes; i++) stats.visits += stats.passLength[i];
@@ -1230,10 +1249,11 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       if (pass == 0) {
         double size = opt.firstBatch ? opt.firstBatch : 16u, b = 0;
         const double growth = (opt.bandGrowth ? opt.bandGrowth : 200u) / 100.0;
+        const double growthLarge = (opt.bandGrowthLarge ? opt.bandGrowthLarge : kDefaultGrowthLarge) / 100.0;
         while (b < end && (int)J.bandEnds.size() < kMaxBands - 1) {
           b = std::min<double>(end, b + std::max(1.0, size));
           J.bandEnds.push_back((int)b);
-          size *= growth;
+          size *= size * 64 < end ? growth : growthLarge;
         }
         if (J.bandEnds.back() < (int)end) J.bandEnds.push_back((int)end);
       } else {
@@ -1312,7 +1332,8 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       J.bettersTotal = c.betters;
       J.passes = pass + 1;
       stats.visits += (unsigned)visited[i];
-      if ((float)betters / J.ntargets < 0.1 && pass + 1 >= (int)opt.minPasses) J.active = false;   // lib/refiner.h:111
+      if ((float)betters / J.ntargets < 0.1 && pass + 1 >= wave_min_passes(opt, J.noContext, J.dp.pb.nm))
+        J.active = false;   // lib/refiner.h:111
     }
   }
   // 4. results: colours back into the caller's layout, one copy per request
