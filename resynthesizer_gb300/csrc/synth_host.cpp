@@ -1750,12 +1750,22 @@ RS_EXPORT int imageSynthBatch(TResynthRequest* requests, unsigned int count, uns
     if (!opt.separateRequests && batch_eligible(requests[i], opt)) multi.push_back(&requests[i]);
     else rest.push_back(i);
   }
+  // Cohorts of at most 2^28 pixels (~10 GB of device state) run one after
+  // the other, so a large batch does not need all its state at once.
   TResynthStats multiStats{};
-  int multiRc = 0;
-  if (!multi.empty()) {
-    multiRc = guarded("imageSynthBatch", [&] { return run_batch_wave(multi, opt, multiStats); });
-    if (multiRc)
-      for (TResynthRequest* r : multi) r->result = multiRc;
+  for (size_t first = 0; first < multi.size();) {
+    size_t last = first;
+    unsigned long long px = 0;
+    while (last < multi.size() &&
+           (last == first || px + (unsigned long long)multi[last]->image->width * multi[last]->image->height <= (1ull << 28))) {
+      px += (unsigned long long)multi[last]->image->width * multi[last]->image->height;
+      last++;
+    }
+    std::vector<TResynthRequest*> cohort(multi.begin() + first, multi.begin() + last);
+    const int rc = guarded("imageSynthBatch", [&] { return run_batch_wave(cohort, opt, multiStats); });
+    if (rc)
+      for (TResynthRequest* r : cohort) r->result = rc;
+    first = last;
   }
   std::atomic<unsigned> next{0};
   auto work = [&] {

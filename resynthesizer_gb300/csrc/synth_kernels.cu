@@ -17,6 +17,7 @@
 //   k_frozen   frozen-state best fit over explicit candidate lists
 //   k_energy   full-patch metric at each target's source
 #include <climits>
+#include <cstddef>
 #include <cstdint>
 #include <map>
 #include <mutex>
@@ -37,6 +38,9 @@ struct Patch {
   int2 src[kMaxNeighbors];       // sourceOf of the neighbour
   int doff[kMaxNeighbors];       // dy * row stride + dx in the padded corpus (wavefront kernel)
 };
+// The fast scoring path reads four consecutive px / map / doff entries at once.
+static_assert(offsetof(Patch, px) % 16 == 0 && offsetof(Patch, map) % 16 == 0 && offsetof(Patch, doff) % 16 == 0,
+              "16-byte patch rows");
 
 // A corpus copy in memory: pixel (x, y) is word y * stride + x + origin.
 struct CorpusView {
@@ -385,7 +389,18 @@ __device__ void score_warp(const Problem& pb, const CorpusView& cv, const uint32
     const bool active = k < ncand;
     if (active) {
       uint32_t add = 0;
-      if (i + 4 <= n) {
+      if (FAST && i + 4 <= n) {
+        // i is a multiple of 4 here: the patch entries of four terms come
+        // in one 16-byte load per array
+        const int4 d4 = *reinterpret_cast<const int4*>(&P.doff[i]);
+        const uint4 p4 = *reinterpret_cast<const uint4*>(&P.px[i]);
+        uint4 m4 = make_uint4(0, 0, 0, 0);
+        if (MAP) m4 = *reinterpret_cast<const uint4*>(&P.map[i]);
+        add = term_at<NC, MAP>(cv, ct, mt, cb + d4.x, true, p4.x, m4.x, pb.nm, pb.clipCost, i == 0) +
+              term_at<NC, MAP>(cv, ct, mt, cb + d4.y, true, p4.y, m4.y, pb.nm, pb.clipCost, false) +
+              term_at<NC, MAP>(cv, ct, mt, cb + d4.z, true, p4.z, m4.z, pb.nm, pb.clipCost, false) +
+              term_at<NC, MAP>(cv, ct, mt, cb + d4.w, true, p4.w, m4.w, pb.nm, pb.clipCost, false);
+      } else if (i + 4 <= n) {
 #pragma unroll
         for (int u = 0; u < 4; u++) add += term(i + u);
       } else {
@@ -762,6 +777,7 @@ struct WaveSmem {
   static constexpr int kPerWarp = (int)sizeof(Patch) + kMaxNeighbors * (int)sizeof(unsigned long long);
   static constexpr int kHead = 2 * 256 * 4 + 16;   // half tables + two mbarriers
 };
+static_assert(WaveSmem::kHead % 16 == 0 && WaveSmem::kPerWarp % 16 == 0, "16-byte aligned warp regions");
 
 // Shared memory and team layout of one CTA of the wavefront kernels: warps
 // form teams of G (a power of two); a team's patch and candidate list live in
