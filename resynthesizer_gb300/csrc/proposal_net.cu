@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(128, 1) k_net_infer(InferArgs a) {
   float* sBias = reinterpret_cast<float*>(sm + kWBytes);
   unsigned char* buf0 = sm + kWBytes + kBiasBytes;
   unsigned char* buf1 = buf0 + kBuf0;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5;
   if (tid == 0) {
     tc::mbar_init1(&barW);
     tc::mbar_init1(&barMma);

@@ -131,10 +131,6 @@ struct Pt {
 
 // Comparators of the reference (lib/engineTypes.h:51-149): they never return
 // 0, so the tie order is libc qsort's -- the reason ordering calls qsort.
-int cmp_less_cartesian(const void* va, const void* vb) {
-  const Pt *a = (const Pt*)va, *b = (const Pt*)vb;
-  return (a->y * a->y + a->x * a->x < b->y * b->y + b->x * b->x) ? -1 : 1;
-}
 int cmp_more_horizontal(const void* va, const void* vb) {
   const Pt *a = (const Pt*)va, *b = (const Pt*)vb;
   return (a->x * a->x < b->x * b->x) ? 1 : -1;
@@ -1626,7 +1622,7 @@ void map_alloc(Map* m, unsigned w, unsigned h, unsigned depth, size_t eltSize) {
   m->height = h;
   m->depth = depth;
   GArray* a = (GArray*)calloc(1, sizeof(GArray));
-  a->data = (char*)calloc((size_t)w * h ? (size_t)w * h : 1, eltSize);
+  a->data = (char*)calloc(std::max<size_t>((size_t)w * h, 1), eltSize);
   a->len = 0;
   m->data = a;
 }
