@@ -312,6 +312,12 @@ const char *resynthLastError(void);
  * even bf16).  N must be a multiple of 32. */
 int resynthTcGemm(const float *A, const float *B, int M, int N, int K, float *D);
 
+/* No counterpart in the reference.  Test entry of the kernels' bounded waits:
+ * runs one GEMM tile whose load barrier can never complete, so its wait gives
+ * up after a fixed number of polls.  Returns RESYNTH_ERROR_DEVICE ("a
+ * tensor-core wait ran out") with the CUDA context still usable. */
+int resynthTcWaitTimeout(void);
+
 /* No counterpart in the reference.  The proposal network reads an 11 x 11
  * context around a target pixel and emits 16 source offsets; in wavefront
  * mode (TResynthOptions.net) they join each visit's candidates next to the

@@ -137,6 +137,7 @@ def lib() -> C.CDLL:
         L.invert_bytemap.argtypes = [P(Map)]
         L.interleave_mask.argtypes = [P(Map), P(Map)]
         L.resynthTcGemm.argtypes = [vp, vp, C.c_int, C.c_int, C.c_int, vp]
+        L.resynthTcWaitTimeout.argtypes = []
         L.resynthPatchNeighbours.argtypes = [vp, u, u, u, vp, u, C.c_int, vp, vp]
         L.resynthNetParamCount.restype = u
         L.resynthNetCreate.argtypes = [u]

@@ -942,6 +942,45 @@ RS_EXPORT int resynthTcGemm(const float* A, const float* B, int M, int N, int K,
   return 0;
 }
 
+// Test entry of the bounded waits: one GEMM tile whose load barrier expects
+// 16 bytes more than its bulk copies bring, so the wait runs out (after 2^16
+// polls); the kernel sets its error flag, frees its tensor memory and returns.
+RS_EXPORT int resynthTcWaitTimeout(void) {
+  uint16_t *dA = nullptr, *dB = nullptr;
+  float* dD = nullptr;
+  unsigned* dErr = nullptr;
+  cudaError_t e = cudaMalloc(&dA, (size_t)kTileM * 16 * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&dB, (size_t)32 * 16 * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&dD, (size_t)kTileM * 32 * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&dErr, 4);
+  if (e == cudaSuccess) e = cudaMemset(dA, 0, (size_t)kTileM * 16 * 2);
+  if (e == cudaSuccess) e = cudaMemset(dB, 0, (size_t)32 * 16 * 2);
+  if (e == cudaSuccess) e = cudaMemset(dErr, 0, 4);
+  if (e == cudaSuccess) {
+    GemmArgs g{};
+    g.A = dA;
+    g.B = dB;
+    g.M = kTileM;
+    g.N = 32;
+    g.K = 16;
+    g.outF = dD;
+    g.ldo = 32;
+    g.err = dErr;
+    g.extraTx = 16;
+    g.waitLimit = 1 << 16;
+    e = launch_gemm(32, g, 1, 1, 1, 0);
+  }
+  unsigned herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&herr, dErr, 4, cudaMemcpyDeviceToHost);
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dD);
+  cudaFree(dErr);
+  if (e != cudaSuccess) return rs_fail(RESYNTH_ERROR_DEVICE, cudaGetErrorString(e));
+  if (herr) return rs_fail(RESYNTH_ERROR_DEVICE, "tc gemm: a tensor-core wait ran out");
+  return 0;
+}
+
 RS_EXPORT unsigned int resynthNetParamCount(void) { return (unsigned)kParams; }
 
 RS_EXPORT void resynthNetDestroy(TResynthNet* net) {

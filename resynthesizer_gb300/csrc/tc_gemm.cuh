@@ -38,6 +38,8 @@ struct GemmArgs {
   uint16_t* outH;            // bf16 bits, row-major, leading dimension ldo, or null
   int ldo;
   unsigned* err;             // bit 2: a wait ran out
+  unsigned extraTx;          // test only: bytes the load barrier expects beyond the copies (0)
+  int waitLimit;             // polls per barrier wait (0 = 2^20)
 };
 
 // Offset in elements of (row r, column k) in a blocked tile of Rt rows and Kc columns.
@@ -157,14 +159,15 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g) {
   const uint32_t bytesA = (uint32_t)kTileM * K * 2, bytesB = (uint32_t)NT * K * 2;
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(&barLoad)),
-                 "r"(bytesA + bytesB)
+                 "r"(bytesA + bytesB + g.extraTx)
                  : "memory");
     bulk_g2s(sA, g.A + blockIdx.x * g.aTile + blockIdx.z * g.aChunk, bytesA, &barLoad);
     bulk_g2s(sB, g.B + blockIdx.y * g.bTile + blockIdx.z * g.bChunk, bytesB, &barLoad);
   }
   // A failed load wait leaves the copies possibly in flight: the second wait
   // below gives them the same bound again before the CTA leaves.
-  bool ok = mbar_wait(&barLoad, 0, 1 << 20);
+  const int limit = g.waitLimit > 0 ? g.waitLimit : 1 << 20;
+  bool ok = mbar_wait(&barLoad, 0, limit);
   ok = __syncthreads_and(ok) != 0;
   if (ok && threadIdx.x == 0) {
     const uint32_t idesc = instr_desc(kTileM, NT);
@@ -176,7 +179,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g) {
     }
     mma_commit(&barMma);
   }
-  bool done = ok ? mbar_wait(&barMma, 0, 1 << 20) : (mbar_wait(&barLoad, 0, 1 << 20), false);
+  bool done = ok ? mbar_wait(&barMma, 0, limit) : (mbar_wait(&barLoad, 0, limit), false);
   done = __syncthreads_and(done) != 0;
   if (!done && threadIdx.x == 0) atomicOr(g.err, 4u);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");

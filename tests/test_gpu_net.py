@@ -22,6 +22,17 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32)
 
 
+def test_bounded_wait_reports_and_context_survives():
+    # a barrier that never completes: the kernel gives up, flags the error and
+    # frees its tensor memory; the next GEMM on the same context is correct
+    rc = R.lib().resynthTcWaitTimeout()
+    assert rc == 100 and "ran out" in R.last_error()
+    a = np.random.default_rng(1).standard_normal((128, 32)).astype(np.float32)
+    d = R.tc_gemm(a, a)
+    ref = bf16(a).astype(np.float64) @ bf16(a).astype(np.float64).T
+    np.testing.assert_allclose(d, ref, rtol=1e-4, atol=1e-3)
+
+
 @pytest.mark.parametrize("m,n,k", [(128, 32, 16), (128, 32, 64), (300, 96, 288), (1000, 32, 80),
                                    (257, 64, 600)])
 def test_tc_gemm_matches_fp32(m, n, k):
