@@ -13,6 +13,8 @@ engine() (wavefront mode), all passes until the reference's termination rule.
   roofline    the per-target synthesis kernel (k_wave), its launches timed live
           with CUDA events on the library stream
   cpu_baseline  the CPU engine on a bounded sample of the workload
+  learned     learned proposals against the plain search on a 1024^2 heal
+          (network trained on the GPU from pairs dumped by plain runs)
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -277,19 +279,18 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
-def run_learned(args):
-    """Learned proposals against the plain search on the large heal (seeded
-    value noise, union of 40 ellipses covering ~10 % of the image): pairs are
-    dumped by plain wavefront runs over `--train-images` images (seeds 1..N),
-    the network trains on the GPU with the tensor-core kernels, then a
+def learned_comparison(size, train_images, train_pairs, train_steps, searches, reps=3):
+    """Learned proposals against the plain search on the large-heal family
+    (seeded value noise, union of 40 ellipses covering ~10 % of the image):
+    pairs are dumped by plain wavefront runs over `train_images` images (seeds
+    1..N), the network trains on the GPU with the tensor-core kernels, then a
     held-out image (seed 0) is synthesized with and without the network's 16
-    proposals at several probe counts.  Energy = sum of the full-patch metric
+    proposals at the given probe counts.  Energy = sum of the full-patch metric
     over the targets at their final sources."""
     import numpy as np
 
     import resynthesizer_gb300 as R
     from resynthesizer_gb300 import workloads as W
-    size = args.learned_size
     fmt = R.format_indices(3, 0, 0, 0, 0)
 
     def run(wl, trys, net=None, dump=None, stride=16, state=True):
@@ -308,21 +309,21 @@ def run_learned(args):
         return r, e
 
     t0 = time.perf_counter()
-    pairs = R.Pairs(args.train_pairs)
-    per_image = max(1, args.train_pairs // args.train_images)
-    for i in range(1, args.train_images + 1):
+    pairs = R.Pairs(train_pairs)
+    per_image = max(1, train_pairs // train_images)
+    for i in range(1, train_images + 1):
         wl = W.heal4096(index=i, size=size)
         run(wl, 200, dump=pairs, stride=max(1, wl["target_px"] // per_image), state=False)
     dump_s = time.perf_counter() - t0
     net = R.Net(seed=1)
     t0 = time.perf_counter()
-    loss = net.train(pairs, steps=args.train_steps, batch=512, lr=1e-3)
+    loss = net.train(pairs, steps=train_steps, batch=512, lr=1e-3)
     train_s = time.perf_counter() - t0
     wl = W.heal4096(index=0, size=size)
     rows = []
-    for trys, use in [(200, False), (64, False), (16, False), (200, True), (64, True), (16, True), (0, True)]:
+    for trys, use in searches:
         ms = []
-        for _ in range(3):
+        for _ in range(reps):
             r, e = run(wl, trys, net=net if use else None)
             ms.append(r.stats["deviceMs"])
         rows.append({"search": ("learned+" if use else "plain ") + f"trys={trys}", "energy": e,
@@ -334,10 +335,19 @@ def run_learned(args):
     # the fastest learned search whose energy is at most the plain search's
     ok = [row for row in rows if row["search"].startswith("learned") and row["energy"] <= base]
     best = max(ok, key=lambda r: r["px_per_s"]) if ok else None
-    line = {"learned": f"heal{size}", "target_px": wl["target_px"], "train_images": args.train_images,
-            "train_pairs": len(pairs), "dump_s": dump_s, "train_steps": args.train_steps, "train_s": train_s,
+    net.close()
+    pairs.close()
+    return {"learned": f"heal{size}", "target_px": wl["target_px"], "train_images": train_images,
+            "train_pairs": train_pairs, "dump_s": dump_s, "train_steps": train_steps, "train_s": train_s,
             "train_loss": loss, "rows": rows,
             "learned_vs_plain_px_per_s_at_equal_energy": (best["px_per_s"] / rows[0]["px_per_s"]) if best else None}
+
+
+def run_learned(args):
+    """The full learned-vs-plain table (see learned_comparison)."""
+    line = learned_comparison(args.learned_size, args.train_images, args.train_pairs, args.train_steps,
+                              [(200, False), (64, False), (16, False), (200, True), (64, True), (16, True),
+                               (0, True)])
     print(json.dumps(line), flush=True)
 
 
@@ -380,6 +390,7 @@ def main():
     ap.add_argument("--quality-runs", type=int, default=3)
     ap.add_argument("--concurrency", type=int, default=8, help="host workers for batch workloads")
     ap.add_argument("--learned", action="store_true", help="learned proposals against the plain search")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain object of the bench line")
     ap.add_argument("--learned-size", type=int, default=4096)
     ap.add_argument("--train-images", type=int, default=64)
     ap.add_argument("--train-pairs", type=int, default=2000000)
@@ -534,6 +545,16 @@ def main():
         stt = cpu_sample(threads=1)
         line["cpu_baseline"] = {"value": mt["value"], "unit": "target px/s", "cores": 8, "kind": mt["kind"],
                                 "sample": mt["sample"], "single_thread_value": stt["value"]}
+    if not args.no_learned and wname == "render1024" and rank == 0:
+        # learned vs plain (outside every timed region above): a 1024^2 heal,
+        # network trained on pairs from four plain runs, 200 probes each way
+        c = learned_comparison(1024, 4, 400000, 1000, [(200, False), (200, True)])
+        plain, learned = c["rows"]
+        line["learned"] = {"workload": "heal1024: seeded value noise, 40 ellipses ~10 %, P=30, trys=200",
+                           "train": {"images": 4, "pairs": c["train_pairs"], "steps": 1000, "seconds": c["train_s"]},
+                           "plain_px_per_s": plain["px_per_s"], "learned_px_per_s": learned["px_per_s"],
+                           "learned_vs_plain_px_per_s": learned["px_per_s"] / plain["px_per_s"],
+                           "learned_energy_vs_plain": learned["energy"] / plain["energy"]}
     print(json.dumps(line), flush=True)
 
 

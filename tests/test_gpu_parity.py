@@ -283,3 +283,54 @@ def test_batch_matches_single_calls(oracle):
     for r, out in zip(reqs[:2], outs):
         rc_o, out_o, _ = oracle.image_synth(r["image"], r["mask"], r["fmt"], op(r["params"]))
         assert rc_o == 0 and (out_o == out).all()
+
+
+@pytest.mark.parametrize("case", ["1x3", "3x3_p0", "5x4_p1", "7x7_p2", "9x6_p64", "tiny_corpus", "tiled_8x8",
+                                  "gray_alpha", "row_16x1"])
+def test_wavefront_edge_cases(case):
+    """Tiny and degenerate problems in wavefront mode: every target gets a
+    source whose colour it carries; the rest of the image is untouched."""
+    rng = np.random.default_rng(len(case))
+    fmt = W.T_RGB
+    patch, tile = 16, (0, 0)
+    if case == "1x3":
+        img = rng.integers(0, 256, (1, 3, 3), dtype=np.uint8)
+        mask = np.array([[0, 255, 0]], np.uint8)
+    elif case == "row_16x1":
+        img = rng.integers(0, 256, (1, 16, 3), dtype=np.uint8)
+        mask = np.zeros((1, 16), np.uint8)
+        mask[0, 5:11] = 255
+    elif case == "tiny_corpus":
+        img = rng.integers(0, 256, (6, 6, 3), dtype=np.uint8)
+        mask = np.full((6, 6), 255, np.uint8)
+        mask[0, 0] = 0                      # a single corpus pixel
+    elif case == "gray_alpha":
+        fmt = W.T_GrayA
+        img = rng.integers(0, 256, (12, 10, 2), dtype=np.uint8)
+        img[..., 1] = 255
+        mask = np.zeros((12, 10), np.uint8)
+        mask[3:8, 2:7] = 255
+    else:
+        h, w = {"3x3_p0": (3, 3), "5x4_p1": (5, 4), "7x7_p2": (7, 7), "9x6_p64": (9, 6), "tiled_8x8": (8, 8)}[case]
+        patch = {"3x3_p0": 0, "5x4_p1": 1, "7x7_p2": 2, "9x6_p64": 64, "tiled_8x8": 9}[case]
+        if case == "tiled_8x8":
+            tile = (1, 1)
+        img = rng.integers(0, 256, (h, w, 3), dtype=np.uint8)
+        mask = np.zeros((h, w), np.uint8)
+        mask[h // 3:h - h // 3, w // 3:w - w // 3] = 255
+    kw = dict(tileH=tile[0], tileV=tile[1], matchContextType=1, patchSize=patch, maxProbeCount=50)
+    tgt, cor = W.simple_to_pixmaps(img, mask)
+    nb = img.shape[2]
+    f = R.format_indices(*{W.T_RGB: (3, 0, 0, 0, 0), W.T_GrayA: (1, 0, 1, 1, 0)}[fmt])
+    r = R.engine(tgt, cor, f, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1))
+    assert r.rc == 0, R.last_error()
+    sel = mask != 0
+    assert (r.out[~sel] == tgt[~sel]).all()
+    src = r.source[sel]
+    assert (src[:, 0] >= 0).all()
+    nc = f.img_match_bpp
+    assert (r.out[sel][:, 1:1 + nc] == cor[src[:, 1], src[:, 0], 1:1 + nc]).all()
+    assert (cor[src[:, 1], src[:, 0], 0] == 255).all()
+    # the Simple API on the same input gives the same colours
+    s = R.image_synth(img, mask, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
+    assert s.rc == 0 and (s.out[..., :nc] == r.out[..., 1:1 + nc]).all()
