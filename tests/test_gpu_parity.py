@@ -334,3 +334,25 @@ def test_wavefront_edge_cases(case):
     # the Simple API on the same input gives the same colours
     s = R.image_synth(img, mask, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
     assert s.rc == 0 and (s.out[..., :nc] == r.out[..., 1:1 + nc]).all()
+
+
+def test_batch_mixed_requests_and_errors(oracle):
+    """One batch with random-order requests (shared launches), directional
+    ones (host workers), replay-equivalent checks and per-request errors."""
+    reqs = W.batch_requests(n=10, lo=40, hi=90, index=11)
+    items = [(r["image"], r["mask"], r["fmt"], R.params(**r["params"])) for r in reqs]
+    # requests 3 and 4 use the brushfire order (workers), 6 has an empty mask, 7 a mask of the wrong size
+    items[3] = (items[3][0], items[3][1], items[3][2], R.params(**dict(reqs[3]["params"], matchContextType=2)))
+    items[4] = (items[4][0], items[4][1], items[4][2], R.params(**dict(reqs[4]["params"], matchContextType=3)))
+    items[6] = (items[6][0], np.zeros_like(items[6][1]), items[6][2], items[6][3])
+    items[7] = (items[7][0], items[7][1][:-1], items[7][2], items[7][3])
+    rc, outs, codes, st = R.image_synth_batch(items, opts=R.options(mode=R.MODE_WAVEFRONT), concurrency=3)
+    assert codes[6] == 5      # IMAGE_SYNTH_ERROR_EMPTY_TARGET
+    assert codes[7] == 2      # IMAGE_SYNTH_ERROR_IMAGE_MASK_MISMATCH
+    assert rc == 5            # the first nonzero request result
+    for i, (img, mask, fmt, p) in enumerate(items):
+        if i in (6, 7):
+            continue
+        assert codes[i] == 0
+        single = R.image_synth(img, mask, fmt, p, opts=R.options(mode=R.MODE_WAVEFRONT))
+        assert single.rc == 0 and (single.out == outs[i]).all(), i
