@@ -341,12 +341,27 @@ __device__ __forceinline__ void load_half_tables(const Problem& pb, uint32_t* ct
 
 __device__ __forceinline__ CorpusView plain_view(const Problem& pb) { return CorpusView{pb.cpx, pb.cmap, pb.cw, 0}; }
 
-// Full patch metric, one thread, stopping once the sum reaches stopAt.
+// Full patch metric, one thread, stopping once the sum reaches stopAt.  The
+// check comes after every eight terms (their loads then overlap): a sum that
+// would have stopped earlier only grows by non-negative terms, so it still
+// reaches stopAt, and a complete sum is the same -- the caller's decision
+// (sum < best, sum == 0) does not change.
 template <int NC, bool MAP>
 __device__ uint32_t patch_sum(const Problem& pb, const CorpusView& cv, const uint32_t* ct, const uint32_t* mt,
                               int cx, int cy, const Patch& P, int n, uint32_t stopAt, unsigned& terms) {
   uint32_t sum = 0;
-  for (int i = 0; i < n; i++) {
+  int i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint32_t g = 0;
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      g += term_cost<NC, MAP>(pb, cv, ct, mt, cx, cy, P.off[i + u], P.px[i + u], MAP ? P.map[i + u] : 0u,
+                              i + u == 0);
+    sum += g;
+    terms += 8;
+    if (sum >= stopAt) return sum;
+  }
+  for (; i < n; i++) {
     sum += term_cost<NC, MAP>(pb, cv, ct, mt, cx, cy, P.off[i], P.px[i], MAP ? P.map[i] : 0u, i == 0);
     terms++;
     if (sum >= stopAt) break;
