@@ -342,28 +342,26 @@ __device__ __forceinline__ void load_half_tables(const Problem& pb, uint32_t* ct
 __device__ __forceinline__ CorpusView plain_view(const Problem& pb) { return CorpusView{pb.cpx, pb.cmap, pb.cw, 0}; }
 
 // Full patch metric, one thread, stopping once the sum reaches stopAt.  The
-// check comes after every eight terms (their loads then overlap): a sum that
-// would have stopped earlier only grows by non-negative terms, so it still
-// reaches stopAt, and a complete sum is the same -- the caller's decision
-// (sum < best, sum == 0) does not change.
-template <int NC, bool MAP>
+// check comes after every G terms, whose loads then overlap (a ragged last
+// group recomputes the final term and adds zero for it): a sum that would have
+// stopped earlier only grows by non-negative terms, so it still reaches
+// stopAt, and a complete sum is the same -- the caller's decision (sum < best,
+// sum == 0) does not change.
+template <int NC, bool MAP, int G = 8>
 __device__ uint32_t patch_sum(const Problem& pb, const CorpusView& cv, const uint32_t* ct, const uint32_t* mt,
                               int cx, int cy, const Patch& P, int n, uint32_t stopAt, unsigned& terms) {
   uint32_t sum = 0;
-  int i = 0;
-  for (; i + 8 <= n; i += 8) {
+  for (int i = 0; i < n; i += G) {
     uint32_t g = 0;
 #pragma unroll
-    for (int u = 0; u < 8; u++)
-      g += term_cost<NC, MAP>(pb, cv, ct, mt, cx, cy, P.off[i + u], P.px[i + u], MAP ? P.map[i + u] : 0u,
-                              i + u == 0);
+    for (int u = 0; u < G; u++) {
+      const int k = min(i + u, n - 1);
+      const uint32_t v =
+          term_cost<NC, MAP>(pb, cv, ct, mt, cx, cy, P.off[k], P.px[k], MAP ? P.map[k] : 0u, i + u == 0);
+      g += i + u < n ? v : 0u;
+    }
     sum += g;
-    terms += 8;
-    if (sum >= stopAt) return sum;
-  }
-  for (; i < n; i++) {
-    sum += term_cost<NC, MAP>(pb, cv, ct, mt, cx, cy, P.off[i], P.px[i], MAP ? P.map[i] : 0u, i == 0);
-    terms++;
+    terms += (unsigned)min(G, n - i);
     if (sum >= stopAt) break;
   }
   return sum;
@@ -690,7 +688,12 @@ __global__ void __launch_bounds__(256, 1) k_replay(ReplayArgs a, int t0, int t1)
         int2 c = make_int2(0, 0);
         if (k < count && P.src[k].x != -1) {
           c = make_int2(P.src[k].x - off_dx(P.off[k]), P.src[k].y - off_dy(P.off[k]));
-          valid = corpus_ok(pb, plain_view(pb), c) && a.recentProber[c.y * pb.cw + c.x] != (unsigned)t;
+          // corpus mask and recentProber are loaded together (no short circuit)
+          const bool inb = (unsigned)c.x < (unsigned)pb.cw && (unsigned)c.y < (unsigned)pb.ch;
+          const int ci = inb ? c.y * pb.cw + c.x : 0;
+          const uint32_t cpx = pb.cpx[ci];
+          const unsigned prober = a.recentProber[ci];
+          valid = inb && (cpx & 0xFFu) == 0xFFu && prober != (unsigned)t;
         }
         const unsigned long long key =
             valid ? ((unsigned long long)(unsigned)c.y << 32 | (unsigned)c.x) : (~0ull - (unsigned)lane);
