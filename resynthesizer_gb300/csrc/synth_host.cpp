@@ -518,10 +518,10 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
   pb.padW = (int)cw + 2 * rs::kPad;
   const size_t padWords = (((size_t)pb.padW * (ch + 2 * rs::kPad)) + 3) & ~(size_t)3;
   uint32_t* cpxPad = ar.alloc<uint32_t>(padWords);
-  uint32_t* cmapPad = pb.nm ? ar.alloc<uint32_t>(padWords) : nullptr;
-  CK(rs_launch_pack_padded(dC, (int)cw, (int)ch, f.total_bpp, pb.nc, f.map_start_bip, pb.nm, cpxPad, cmapPad, s));
+  uint2* cpmPad = pb.nm ? ar.alloc<uint2>(padWords) : nullptr;
+  CK(rs_launch_pack_padded(dC, (int)cw, (int)ch, f.total_bpp, pb.nc, f.map_start_bip, pb.nm, cpxPad, cpmPad, s));
   pb.cpxPad = cpxPad;
-  pb.cmapPad = cmapPad;
+  pb.cpmPad = cpmPad;
   launches += 3;
   pb.tpx = d.tpx;
   pb.tmap = d.tmap;

@@ -28,7 +28,7 @@ struct Problem {
   const uint32_t* cpx;        // corpus pixels (cw*ch)
   const uint32_t* cmap;       // corpus map channels (cw*ch) or null
   const uint32_t* cpxPad;     // the corpus with a kPad-wide masked border ((cw+2kPad) x (ch+2kPad))
-  const uint32_t* cmapPad;    // ... and its map channels, or null
+  const uint2* cpmPad;        // with map channels: the padded corpus as (corpus word, map word) pairs, else null
   int padW;                   // cw + 2 * kPad
   const int2* cpts;           // corpus points (selected and not transparent)
   int ncorpus;
@@ -116,7 +116,7 @@ extern "C" {
 cudaError_t rs_launch_pack(const uint8_t* raw, int w, int h, int bpp, int colorStart, int nc, int mapStart,
                            int nm, uint32_t* px, uint32_t* map, cudaStream_t s);
 cudaError_t rs_launch_pack_padded(const uint8_t* raw, int w, int h, int bpp, int nc, int mapStart, int nm,
-                                  uint32_t* px, uint32_t* map, cudaStream_t s);
+                                  uint32_t* px, uint2* pm, cudaStream_t s);
 cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc, const uint32_t* px,
                                     cudaStream_t s);
 cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream_t s);

@@ -42,12 +42,34 @@ struct Patch {
 static_assert(offsetof(Patch, px) % 16 == 0 && offsetof(Patch, map) % 16 == 0 && offsetof(Patch, doff) % 16 == 0,
               "16-byte patch rows");
 
-// A corpus copy in memory: pixel (x, y) is word y * stride + x + origin.
+// A corpus copy in memory: pixel (x, y) is element y * stride + x + origin.
+// CorpusView keeps corpus words and map words in separate arrays (the plain
+// corpus; the padded corpus of problems without maps); PairView holds the
+// padded corpus of problems with maps as (corpus word, map word) pairs, so a
+// term is one 8-byte load.
 struct CorpusView {
   const uint32_t* px;
   const uint32_t* map;
   int stride, origin;
 };
+struct PairView {
+  const uint2* pm;
+  int stride, origin;
+};
+
+template <bool MAP>
+__device__ __forceinline__ void view_load(const CorpusView& v, int qi, uint32_t& s, uint32_t& m) {
+  s = v.px[qi];
+  m = MAP ? v.map[qi] : 0u;
+}
+template <bool MAP>
+__device__ __forceinline__ void view_load(const PairView& v, int qi, uint32_t& s, uint32_t& m) {
+  const uint2 w = v.pm[qi];
+  s = w.x;
+  m = w.y;
+}
+__device__ __forceinline__ uint32_t view_px(const CorpusView& v, int qi) { return v.px[qi]; }
+__device__ __forceinline__ uint32_t view_px(const PairView& v, int qi) { return v.pm[qi].x; }
 
 __device__ __forceinline__ int pack_off(int dx, int dy) { return (int)((unsigned)dy << 16 | ((unsigned)dx & 0xffffu)); }
 __device__ __forceinline__ int off_dx(int o) { return (int)(short)(o & 0xffff); }
@@ -305,24 +327,25 @@ constexpr int kScanCap = 512;
 // The metric tables are symmetric (they are functions of d * d, and negation
 // is exact), so ct/mt here are their upper halves, indexed by |t - s|: one
 // SIMD absolute difference gives every channel's index at once.
-template <int NC, bool MAP>
-__device__ __forceinline__ uint32_t term_at(const CorpusView& cv, const uint32_t* ct, const uint32_t* mt, int qi,
+template <int NC, bool MAP, class V>
+__device__ __forceinline__ uint32_t term_at(const V& cv, const uint32_t* ct, const uint32_t* mt, int qi,
                                             bool inb, uint32_t t, uint32_t tm, int nm, uint32_t clip, bool self) {
-  const uint32_t s = cv.px[qi];
+  uint32_t s, sm;
+  view_load<MAP>(cv, qi, s, sm);
   const uint32_t ad = __vabsdiffu4(t, s);
   uint32_t sum = ct[(ad >> 8) & 0xFFu];
   if (NC >= 2) sum += ct[(ad >> 16) & 0xFFu];
   if (NC >= 3) sum += ct[ad >> 24];
   if (self) sum = 0;
   if (MAP) {
-    const uint32_t am = __vabsdiffu4(tm, cv.map[qi]);
+    const uint32_t am = __vabsdiffu4(tm, sm);
     for (int c = 0; c < nm; c++) sum += mt[(am >> (8 * c)) & 0xFFu];
   }
   return (inb && (s & 0xFFu) == 0xFFu) ? sum : clip;
 }
 
-template <int NC, bool MAP>
-__device__ __forceinline__ uint32_t term_cost(const Problem& pb, const CorpusView& cv, const uint32_t* ct,
+template <int NC, bool MAP, class V>
+__device__ __forceinline__ uint32_t term_cost(const Problem& pb, const V& cv, const uint32_t* ct,
                                               const uint32_t* mt, int cx, int cy, int off, uint32_t t, uint32_t tm,
                                               bool self) {
   const int qx = cx + off_dx(off), qy = cy + off_dy(off);
@@ -376,8 +399,8 @@ __device__ uint32_t patch_sum(const Problem& pb, const CorpusView& cv, const uin
 // FAST: every candidate is a corpus point and every patch offset lies within
 // kPad, so with the padded view each term is one load at a precomputed
 // linear offset (the masked border supplies the clip penalty).
-template <int NC, bool MAP, bool FAST, class Get>
-__device__ void score_warp(const Problem& pb, const CorpusView& cv, const uint32_t* ct, const uint32_t* mt,
+template <int NC, bool MAP, bool FAST, class V, class Get>
+__device__ void score_warp(const Problem& pb, const V& cv, const uint32_t* ct, const uint32_t* mt,
                            const Patch& P, int n, int ncand, Get get, int lane, uint32_t& bestVal, int& bestIdx,
                            unsigned& terms, unsigned& evals) {
   bestVal = 0xFFFFFFFFu;
@@ -484,9 +507,17 @@ __device__ __forceinline__ int2 probe_point(const Problem& pb, uint32_t base, ui
   return __ldg(&pb.cpts[__umulhi(h, (uint32_t)pb.ncorpus)]);
 }
 
-__device__ __forceinline__ bool corpus_ok(const Problem& pb, const CorpusView& cv, int2 c) {
+template <class V>
+__device__ __forceinline__ bool corpus_ok(const Problem& pb, const V& cv, int2 c) {
   return (unsigned)c.x < (unsigned)pb.cw && (unsigned)c.y < (unsigned)pb.ch &&
-         (cv.px[c.y * cv.stride + c.x + cv.origin] & 0xFFu) == 0xFFu;
+         (view_px(cv, c.y * cv.stride + c.x + cv.origin) & 0xFFu) == 0xFFu;
+}
+
+// The padded corpus view of a problem (kPad-wide masked border).
+template <bool MAP>
+__device__ __forceinline__ auto padded_view(const Problem& pb) {
+  if constexpr (MAP) return PairView{pb.cpmPad, pb.padW, kPad * pb.padW + kPad};
+  else return CorpusView{pb.cpxPad, nullptr, pb.padW, kPad * pb.padW + kPad};
 }
 
 // ----------------------------------------------------------- shared memory
@@ -818,8 +849,8 @@ struct WaveTeam {
 // network) the network's proposals, then `trys` counter-based random probes;
 // the best (first strict minimum) different source is stored in place, or
 // staged for k_commit.  Returns 1 if the target's source changed (in place).
-template <int NC, bool MAP>
-__device__ __forceinline__ unsigned wave_target(const WaveArgs& a, const Problem& pb, const CorpusView& cv,
+template <int NC, bool MAP, class V>
+__device__ __forceinline__ unsigned wave_target(const WaveArgs& a, const Problem& pb, const V& cv,
                                                 const uint32_t* ct, const uint32_t* mt, int batch, int visCur,
                                                 int b0, int slot, bool sparse, const WaveTeam& T, unsigned& terms,
                                                 unsigned& evals) {
@@ -984,24 +1015,26 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   const Problem& pb = a.pb;
   // The padded corpus: staged into shared memory when it fits.
   const int padH = pb.ch + 2 * kPad;
-  CorpusView cv{pb.cpxPad, pb.cmapPad, pb.padW, kPad * pb.padW + kPad};
+  auto cv = padded_view<MAP>(pb);
   const unsigned cwords = ((unsigned)(pb.padW * padH) + 3u) & ~3u;
   if (SMEMC) {
-    uint32_t* scpx = reinterpret_cast<uint32_t*>(p);
-    p += cwords * 4;
-    uint32_t* scmap = nullptr;
-    if (MAP) {
-      scmap = reinterpret_cast<uint32_t*>(p);
+    bool ok;
+    if constexpr (MAP) {
+      uint2* scpm = reinterpret_cast<uint2*>(p);
+      p += cwords * 8;
+      ok = stage_words(reinterpret_cast<uint32_t*>(scpm), reinterpret_cast<const uint32_t*>(pb.cpmPad), cwords * 2,
+                       bar);
+      cv.pm = scpm;
+    } else {
+      uint32_t* scpx = reinterpret_cast<uint32_t*>(p);
       p += cwords * 4;
+      ok = stage_words(scpx, pb.cpxPad, cwords, bar);
+      cv.px = scpx;
     }
-    bool ok = stage_words(scpx, pb.cpxPad, cwords, bar);
-    if (MAP && ok) ok = stage_words(scmap, pb.cmapPad, cwords, bar + 1);
     if (!ok) {
       if (threadIdx.x == 0) atomicOr(&a.ctr->error, 1u);
       return;
     }
-    cv.px = scpx;
-    cv.map = scmap;
   }
   __shared__ int s_abort;
   load_half_tables(pb, ct, mt);
@@ -1071,7 +1104,7 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi(const WaveArgs* jobs, int
     const int r = multi_request(prefix, nreq, gs);
     const WaveArgs& a = jobs[r];
     const Problem& pb = a.pb;
-    const CorpusView cv{pb.cpxPad, pb.cmapPad, pb.padW, kPad * pb.padW + kPad};
+    const auto cv = padded_view<MAP>(pb);
     const int b0 = a.batchStart[step];
     const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
     unsigned terms = 0, evals = 0;
@@ -1187,7 +1220,7 @@ __global__ void k_pack(const uint8_t* raw, int npx, int bpp, int colorStart, int
 
 // The corpus with a kPad-wide border of zero (masked) words.
 __global__ void k_pack_padded(const uint8_t* raw, int w, int h, int bpp, int nc, int mapStart, int nm,
-                              uint32_t* px, uint32_t* map) {
+                              uint32_t* px, uint2* pm) {
   const int pw = w + 2 * kPad, ph = h + 2 * kPad;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < pw * ph; i += gridDim.x * blockDim.x) {
     const int x = i % pw - kPad, y = i / pw - kPad;
@@ -1199,7 +1232,7 @@ __global__ void k_pack_padded(const uint8_t* raw, int w, int h, int bpp, int nc,
       for (int c = 0; c < nm; c++) m |= (uint32_t)q[mapStart + c] << (8 * c);
     }
     px[i] = word;
-    if (map) map[i] = m;
+    if (pm) pm[i] = make_uint2(word, m);
   }
 }
 
@@ -1253,9 +1286,9 @@ extern "C" cudaError_t rs_launch_pack(const uint8_t* raw, int w, int h, int bpp,
 }
 
 extern "C" cudaError_t rs_launch_pack_padded(const uint8_t* raw, int w, int h, int bpp, int nc, int mapStart,
-                                             int nm, uint32_t* px, uint32_t* map, cudaStream_t s) {
+                                             int nm, uint32_t* px, uint2* pm, cudaStream_t s) {
   const int n = (w + 2 * kPad) * (h + 2 * kPad);
-  k_pack_padded<<<grid_for(n, 256, sm_count() * 8), 256, 0, s>>>(raw, w, h, bpp, nc, mapStart, nm, px, map);
+  k_pack_padded<<<grid_for(n, 256, sm_count() * 8), 256, 0, s>>>(raw, w, h, bpp, nc, mapStart, nm, px, pm);
   return cudaGetLastError();
 }
 
