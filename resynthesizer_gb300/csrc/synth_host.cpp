@@ -561,8 +561,6 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
   return d;
 }
 
-// Radius (squared) of the offset list used by the wavefront mode: enough for
-// any dense patch; sparse early batches look this far for context.
 // Growth of the large pass-0 bands (percent): once a band holds 1/64 of the
 // pass, bands grow more slowly, so that fewer targets share a batch when the
 // neighbourhoods are dense (energy); the small bands before are latency-bound
@@ -601,6 +599,8 @@ void set_tuned_warps(uint64_t key, int warps) {
   g_tunedWarps[key] = warps;
 }
 
+// Radius (squared) of the offset list used by the wavefront mode: enough for
+// any dense patch; sparse early batches look this far for context.
 long long wave_radius2(int w, int h) {
   const long long full = (long long)(w - 1) * (w - 1) + (long long)(h - 1) * (h - 1);
   return std::min<long long>(full, 256LL * 256LL);

@@ -214,20 +214,26 @@ __device__ void merge_keys(unsigned long long* best, int& cnt, unsigned long lon
 // parts' lists gives the whole list's lim smallest keys.
 __device__ void sparse_keys(const Problem& pb, int px, int py, unsigned long long* best, int& cnt,
                             unsigned long long& thr, const int2* list, int V, int lane, int part, int parts) {
+  constexpr int kU = 4;   // list loads per lane in flight
   const int lim = pb.patchLimit - 1;
   const int bw = pb.boxW, bh = pb.boxH;
-  for (int base = part * 32; base < V; base += 32 * parts) {
-    const int j = base + lane;
-    unsigned long long key = ~0ull;
-    if (j < V) {
-      const int2 q = list[j];
-      const int dx = q.x - px, dy = q.y - py;
-      if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
-        const long long d2 = (long long)dx * dx + (long long)dy * dy;
-        if (d2 <= pb.maxD2) key = offset_key(pb, dx, dy);
+  for (int base = part * 32; base < V; base += 32 * parts * kU) {
+    unsigned long long key[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const int j = base + 32 * parts * u + lane;
+      key[u] = ~0ull;
+      if (j < V) {
+        const int2 q = list[j];
+        const int dx = q.x - px, dy = q.y - py;
+        if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
+          const long long d2 = (long long)dx * dx + (long long)dy * dy;
+          if (d2 <= pb.maxD2) key[u] = offset_key(pb, dx, dy);
+        }
       }
     }
-    topk_insert(key, best, cnt, thr, lim, lane);
+#pragma unroll
+    for (int u = 0; u < kU; u++) topk_insert(key[u], best, cnt, thr, lim, lane);
   }
 }
 
@@ -286,24 +292,33 @@ __device__ void grid_keys(const Problem& pb, int px, int py, unsigned long long*
         }
       }
       unsigned wm = __ballot_sync(kFull, want);
+      // Four wanted cells per warp pass: lanes 8g .. 8g+7 read the eight rows
+      // of cell g, eight pixels each, all loads in flight at once.
+      static_assert(kCell == 8, "8 x 8 cells");
+      const int g = lane >> 3, row = lane & 7;
       while (wm) {
-        const int src = __ffs(wm) - 1;
-        wm &= wm - 1;
-        const int scx = __shfl_sync(kFull, qcx, src), scy = __shfl_sync(kFull, qcy, src);
-        // lane: row lane / 4 of the cell, 2 columns from (lane & 3) * 2
-        static_assert(kCell == 8, "one 8 x 8 cell per warp pass");
-        const int qy = (scy << kCellShift) + (lane >> 2);
-        const int qx0 = (scx << kCellShift) + (lane & 3) * 2;
+        int src = -1;
 #pragma unroll
-        for (int j = 0; j < 2; j++) {
-          const int qx = qx0 + j, dx = qx - px, dy = qy - py;
-          unsigned long long key = ~0ull;
-          if (qx < pb.tw && qy < pb.th && dx > -bw && dx < bw && dy > -bh && dy < bh) {
-            const long long d2 = (long long)dx * dx + (long long)dy * dy;
-            if (d2 <= pb.maxD2 && pb.vis[qy * pb.tw + qx] < visCur) key = offset_key(pb, dx, dy);
+        for (int t = 0; t < 4; t++) {
+          if (wm) {
+            if (t == g) src = __ffs(wm) - 1;
+            wm &= wm - 1;
           }
-          topk_insert(key, best, cnt, thr, lim, lane);
         }
+        const int scx = __shfl_sync(kFull, qcx, src < 0 ? 0 : src), scy = __shfl_sync(kFull, qcy, src < 0 ? 0 : src);
+        const int qy = (scy << kCellShift) + row, dy = qy - py;
+        unsigned long long key[kCell];
+#pragma unroll
+        for (int j = 0; j < kCell; j++) {
+          const int qx = (scx << kCellShift) + j, dx = qx - px;
+          key[j] = ~0ull;
+          if (src >= 0 && qx < pb.tw && qy < pb.th && dx > -bw && dx < bw && dy > -bh && dy < bh) {
+            const long long d2 = (long long)dx * dx + (long long)dy * dy;
+            if (d2 <= pb.maxD2 && pb.vis[qy * pb.tw + qx] < visCur) key[j] = offset_key(pb, dx, dy);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < kCell; j++) topk_insert(key[j], best, cnt, thr, lim, lane);
       }
     }
   }
@@ -320,6 +335,7 @@ __device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, uns
 
 // Offsets walked before a pass-0 patch falls back to the cell grid.
 constexpr int kScanCap = 512;
+
 
 // One neighbour term of computeBestFit for candidate (cx, cy): the clip/mask
 // penalty, or the colour terms (skipped for the target itself) plus the map
