@@ -34,8 +34,26 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "render1024: 128x128 RGBA tile -> 1024x1024 target, random order, P=16, trys=300, engine()"
 METRIC = "target px/s + candidate evals/s; learned vs plain GPU search at equal patch energy"
-TERM_BYTES = 4 + 2 * 3            # corpus word (mask + RGB) + three 16-bit table reads per neighbour term
-TERM_OPS = 4 + 3 * 3              # bounds/mask + (sub, index, add) per colour channel
+
+
+def term_bytes(nc: int, nm: int) -> int:
+    """Algorithmic bytes of one neighbour term: the 4-byte corpus word (mask +
+    colours), a 16-bit table read per colour channel, and per map channel the
+    map byte and a 32-bit table read."""
+    return 4 + 2 * nc + (1 + 4) * nm
+
+
+def term_ops(nc: int, nm: int) -> int:
+    """Integer ops of one neighbour term: bounds/mask, then (sub, index, add)
+    per colour and map channel."""
+    return 4 + 3 * (nc + nm)
+
+# DRAM bytes (read + write) per k_wave launch, the mean over one synthesis, from
+# an ncu launch list (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of
+#   python bench.py --profile-once --no-cpu --warps 16 --workload W
+# ncu flushes the caches before each launch, so these are cold-cache figures:
+# an upper bound for the warm launches timed here.
+WAVE_DRAM_BYTES = {"render1024": 6.64e6, "heal4096": 67.63e6, "mapstyle2048": 28.58e6}
 SAMPLE_SIDE = 256                 # CPU sample: 256x256 target from the same tile
 
 
@@ -382,6 +400,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--warps", type=int, default=0,
+                    help="warps per CTA of the synthesis kernel (0 = autotuned; fix it when profiling, since the "
+                         "tuner's timings are not meaningful under a profiler)")
     ap.add_argument("--profile-once", action="store_true",
                     help="one warm-up and one timed engineDevice call only (for ncu captures)")
     ap.add_argument("--workload", default="render1024",
@@ -443,7 +464,7 @@ def main():
     c_dev = torch.from_numpy(wl["corpus"]).to(dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > 129 MB L2
     stream = torch.cuda.current_stream()
-    opts = R.options(mode=R.MODE_WAVEFRONT)
+    opts = R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=args.warps)
 
     def step(o=opts):
         t_work.copy_(t_init)
@@ -504,10 +525,11 @@ def main():
     # dominant kernel: the per-target synthesis launches, timed live
     flush.fill_(1)
     torch.cuda.synchronize()
-    prof = step(R.options(mode=R.MODE_WAVEFRONT, profile=1))
+    prof = step(R.options(mode=R.MODE_WAVEFRONT, profile=1, warpsPerBlock=args.warps))
     wave_ms_per_launch = prof["waveMs"] / max(1, prof["waveLaunches"])
     terms_per_launch = prof["waveTerms"] / max(1, prof["waveLaunches"])
-    achieved_gbs = terms_per_launch * TERM_BYTES / (wave_ms_per_launch / 1000.0) / 1e9
+    tb, to = term_bytes(fmt.img_match_bpp, fmt.map_match_bpp), term_ops(fmt.img_match_bpp, fmt.map_match_bpp)
+    achieved_gbs = terms_per_launch * tb / (wave_ms_per_launch / 1000.0) / 1e9
     peak, peak_kind = peaks()
 
     # quality of this run (outside every timed region)
@@ -533,10 +555,10 @@ def main():
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": "target px/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
-                     "frac": achieved_gbs / peak, "traffic": None, "kernel": "k_wave",
+                     "frac": achieved_gbs / peak, "traffic": WAVE_DRAM_BYTES.get(wname), "kernel": "k_wave",
                      "peak_kind": peak_kind, "launches": prof["waveLaunches"],
                      "ms_per_launch": wave_ms_per_launch, "terms_per_launch": terms_per_launch,
-                     "bytes_per_term": TERM_BYTES, "int_ops_per_s": terms_per_launch * TERM_OPS /
+                     "bytes_per_term": tb, "int_ops_per_s": terms_per_launch * to /
                      (wave_ms_per_launch / 1000.0)},
         "clocks": clk.summary(),
     }
