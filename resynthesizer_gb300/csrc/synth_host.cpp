@@ -332,6 +332,44 @@ struct Stream {
   int* abortDev = nullptr;
   rs::Counters* hostCtr = nullptr;   // pinned: counter read-backs stay asynchronous
   int* hostInts = nullptr;           // pinned: small read-backs
+  // Side streams for the many-request path: the per-request preparation
+  // kernels (small, independent) run on them side by side, forked from and
+  // joined back into s with events.
+  int* hostBands = nullptr;          // pinned: per-pass band boundaries of every request of a batch
+  size_t hostBandsCap = 0;
+  int* host_bands(size_t n) {
+    if (n > hostBandsCap) {
+      if (hostBands) CK(cudaFreeHost(hostBands));
+      hostBands = nullptr;
+      CK(cudaHostAlloc((void**)&hostBands, n * sizeof(int), cudaHostAllocDefault));
+      hostBandsCap = n;
+    }
+    return hostBands;
+  }
+  static constexpr int kSide = 8;
+  cudaStream_t side[kSide] = {};
+  cudaEvent_t fork = nullptr, join[kSide] = {};
+  void ensure_side() {
+    if (fork) return;
+    for (int i = 0; i < kSide; i++) {
+      CK(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  }
+  // Side streams wait for everything queued on s so far.
+  void fork_side() {
+    ensure_side();
+    CK(cudaEventRecord(fork, s));
+    for (int i = 0; i < kSide; i++) CK(cudaStreamWaitEvent(side[i], fork, 0));
+  }
+  // s waits for everything queued on the side streams.
+  void join_side() {
+    for (int i = 0; i < kSide; i++) {
+      CK(cudaEventRecord(join[i], side[i]));
+      CK(cudaStreamWaitEvent(s, join[i], 0));
+    }
+  }
   Stream() {
     CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     CK(cudaHostAlloc((void**)&abortHost, sizeof(int), cudaHostAllocMapped));
@@ -368,9 +406,12 @@ Stream& thread_stream() {
 // (fewer address-translation misses when one kernel touches all of them).
 class Arena {
  public:
-  explicit Arena(cudaStream_t s, size_t chunk = 0) : s_(s), chunk_(chunk) {}
+  // Allocations are ordered on s; frees on freeStream (default s), which must
+  // by then be ordered after every use.
+  explicit Arena(cudaStream_t s, size_t chunk = 0, cudaStream_t freeStream = nullptr)
+      : s_(s), free_(freeStream ? freeStream : s), chunk_(chunk) {}
   ~Arena() {
-    for (void* p : ptrs_) cudaFreeAsync(p, s_);
+    for (void* p : ptrs_) cudaFreeAsync(p, free_);
   }
   template <class T>
   T* alloc(size_t n) {
@@ -400,7 +441,7 @@ class Arena {
   }
 
  private:
-  cudaStream_t s_;
+  cudaStream_t s_, free_;
   size_t chunk_ = 0, used_ = 0;
   void* cur_ = nullptr;
   std::vector<void*> ptrs_;
@@ -1092,6 +1133,22 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
   CK(cudaEventCreateWithFlags(&epass, cudaEventDisableTiming));
   CK(cudaEventRecord(e0, s));
   *st.abortHost = 0;
+  // Requests' uploads and preparation run on the side streams, each with its
+  // own arena; on every way out, s first waits for the side streams, then the
+  // side arenas free on s.
+  struct SideArenas {
+    Stream& st;
+    std::vector<std::unique_ptr<Arena>> a;
+    ~SideArenas() {
+      try {
+        st.join_side();
+      } catch (...) {
+      }
+    }
+  } side{st, {}};
+  st.fork_side();
+  for (int q = 0; q < Stream::kSide; q++) side.a.emplace_back(new Arena(st.side[q], (size_t)64 << 20, s));
+  int nextSide = 0;
   // 1. host checks (the reference's order), upload, adaption, preparation
   for (size_t i = 0; i < reqs.size(); i++) {
     BatchJob& J = jobs[i];
@@ -1133,23 +1190,26 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       R.result = IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
       continue;
     }
+    const int sq = nextSide++ % Stream::kSide;
+    const cudaStream_t q = st.side[sq];
+    Arena& qa = *side.a[sq];
     J.imgBytes = img->rowBytes * (h - 1) + (size_t)w * J.bpp;
     const size_t mBytes = R.mask->rowBytes * (h - 1) + w;
-    J.dImg = ar.alloc<uint8_t>(img->rowBytes * h);
-    uint8_t* dMask = ar.alloc<uint8_t>(R.mask->rowBytes * h);
-    uint8_t* dMask2 = R.mask2 ? ar.alloc<uint8_t>(R.mask2->rowBytes * h) : nullptr;
-    CK(cudaMemcpyAsync(J.dImg, img->data, J.imgBytes, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(dMask, R.mask->data, mBytes, cudaMemcpyHostToDevice, s));
+    J.dImg = qa.alloc<uint8_t>(img->rowBytes * h);
+    uint8_t* dMask = qa.alloc<uint8_t>(R.mask->rowBytes * h);
+    uint8_t* dMask2 = R.mask2 ? qa.alloc<uint8_t>(R.mask2->rowBytes * h) : nullptr;
+    CK(cudaMemcpyAsync(J.dImg, img->data, J.imgBytes, cudaMemcpyHostToDevice, q));
+    CK(cudaMemcpyAsync(dMask, R.mask->data, mBytes, cudaMemcpyHostToDevice, q));
     h2d += J.imgBytes + mBytes;
     if (R.mask2) {
       const size_t m2Bytes = R.mask2->rowBytes * (h - 1) + w;
-      CK(cudaMemcpyAsync(dMask2, R.mask2->data, m2Bytes, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(dMask2, R.mask2->data, m2Bytes, cudaMemcpyHostToDevice, q));
       h2d += m2Bytes;
     }
-    J.dT = ar.alloc<uint8_t>((size_t)w * h * d);
-    uint8_t* dC = ar.alloc<uint8_t>((size_t)w * h * d);
+    J.dT = qa.alloc<uint8_t>((size_t)w * h * d);
+    uint8_t* dC = qa.alloc<uint8_t>((size_t)w * h * d);
     CK(rs_adapt(J.dImg, img->rowBytes, dMask, R.mask->rowBytes, dMask2, R.mask2 ? R.mask2->rowBytes : 0, (int)w,
-                (int)h, (int)J.bpp, J.dT, dC, s));
+                (int)h, (int)J.bpp, J.dT, dC, q));
     const long long maxD2 = wave_radius2((int)w, (int)h);
     int nWave = 0;
     const int2* dWave = wave_offsets_device(nWave);
@@ -1158,19 +1218,20 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
                     return (long long)o.x * o.x + (long long)o.y * o.y <= maxD2;
                   }) - wl.begin());
     const std::vector<int2> noList;
-    J.dp = make_problem(ar, s, J.p, J.f, J.dT, w, h, dC, w, h, nullptr, nullptr, noList, maxD2, h2d, launches, dWave,
+    J.dp = make_problem(qa, q, J.p, J.f, J.dT, w, h, dC, w, h, nullptr, nullptr, noList, maxD2, h2d, launches, dWave,
                         nWave);
     const size_t tn = (size_t)w * h;
-    int* scratch = ar.alloc<int>((size_t)rs_prep_scratch_ints((int)w, (int)h));
-    J.dCounts = ar.alloc<int>(4);
-    J.dTargets = ar.alloc<int2>(tn);
-    J.cpts = ar.alloc<int2>(tn);
+    int* scratch = qa.alloc<int>((size_t)rs_prep_scratch_ints((int)w, (int)h));
+    J.dCounts = qa.alloc<int>(4);
+    J.dTargets = qa.alloc<int2>(tn);
+    J.cpts = qa.alloc<int2>(tn);
     CK(rs_prep_target(J.dT, (int)w, (int)h, J.f.total_bpp, J.f.alpha_bip, J.f.isAlphaTarget ? 1 : 0,
-                      J.p.matchContextType ? 1 : 0, J.dp.pb.has, J.dp.pb.src, scratch, J.dTargets, J.dCounts, s));
+                      J.p.matchContextType ? 1 : 0, J.dp.pb.has, J.dp.pb.src, scratch, J.dTargets, J.dCounts, q));
     CK(rs_prep_corpus(dC, (int)w, (int)h, J.f.total_bpp, J.f.alpha_bip, J.f.isAlphaSource ? 1 : 0, scratch, J.cpts,
-                      J.dCounts + 2, s));
+                      J.dCounts + 2, q));
     launches += 8;
   }
+  st.join_side();
   // 2. target and corpus counts of every request: one synchronisation
   std::vector<int> counts(4 * jobs.size(), 0);
   for (size_t i = 0; i < jobs.size(); i++)
@@ -1178,6 +1239,8 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
   CK(cudaStreamSynchronize(s));
   rs::Counters* ctrs = ar.alloc<rs::Counters>(jobs.size());
   CK(cudaMemsetAsync(ctrs, 0, jobs.size() * sizeof(rs::Counters), s));
+  // every request's band boundaries and phase flags, uploaded once per pass
+  int* dBands = ar.alloc<int>(jobs.size() * 2 * kMaxBands);
   for (size_t i = 0; i < jobs.size(); i++) {
     BatchJob& J = jobs[i];
     if (!J.dCounts) continue;
@@ -1210,8 +1273,8 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
     J.batchStart = ar.alloc<int>((size_t)kMaxBands * J.k * J.k + 1);
     J.work = ar.alloc<int>(rs_prep_batches_ints((int)J.ntargets, kMaxBands * J.k * J.k));
     J.dPass = ar.alloc<int2>(J.ntargets);
-    J.dBandEnds = ar.alloc<int>(kMaxBands);
-    J.dBandPhased = ar.alloc<int>(kMaxBands);
+    J.dBandEnds = dBands + i * 2 * kMaxBands;
+    J.dBandPhased = J.dBandEnds + kMaxBands;
     rs::WaveArgs& wa = J.wa;
     wa.pb = pb;
     wa.trys = J.p.maxProbeCount;
@@ -1236,9 +1299,10 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
     for (size_t i = 0; i < jobs.size(); i++)
       if (jobs[i].active) act.push_back(i);
     if (act.empty()) break;
+    // Band boundaries of the pass for every active request, one upload.
+    int* hb = st.host_bands(jobs.size() * 2 * kMaxBands);
     for (size_t i : act) {
       BatchJob& J = jobs[i];
-      const int k = J.k;
       const unsigned end = J.ends[pass];
       // pass-0 bands grow 2x from 16 (random orders); later passes one band
       J.bandEnds.clear();
@@ -1256,18 +1320,30 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
         const unsigned refine = opt.refineBatches ? opt.refineBatches : 1u;
         for (unsigned r = 1; r <= refine; r++) J.bandEnds.push_back((int)((unsigned long long)end * r / refine));
       }
+      int* h = hb + i * 2 * kMaxBands;
+      std::copy(J.bandEnds.begin(), J.bandEnds.end(), h);
+      std::fill(h + kMaxBands, h + kMaxBands + J.bandEnds.size(), 1);
+    }
+    CK(cudaMemcpyAsync(dBands, hb, jobs.size() * 2 * kMaxBands * sizeof(int), cudaMemcpyHostToDevice, s));
+    h2d += jobs.size() * 2 * kMaxBands * sizeof(int);
+    // Per-request preparation of the pass on the side streams (every buffer
+    // it touches was allocated, and the boundaries uploaded, on s before the
+    // fork).
+    st.fork_side();
+    for (size_t ai = 0; ai < act.size(); ai++) {
+      const size_t i = act[ai];
+      const cudaStream_t q = st.side[ai % Stream::kSide];
+      BatchJob& J = jobs[i];
+      const int k = J.k;
+      const unsigned end = J.ends[pass];
       const int nb = (int)J.bandEnds.size();
-      const std::vector<int> phased(nb, 1);
-      CK(cudaMemcpyAsync(J.dBandEnds, J.bandEnds.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
-      CK(cudaMemcpyAsync(J.dBandPhased, phased.data(), nb * sizeof(int), cudaMemcpyHostToDevice, s));
-      h2d += 2 * nb * sizeof(int);
       CK(rs_prep_batches(J.dTargets, (int)J.ntargets, (int)J.w, (int)end, 1, J.wa.seed ^ 0x5bd1e995u, J.dBandEnds,
-                         J.dBandPhased, nb, k, J.work, J.batchStart, J.dPass, pass == 0 ? J.vis : nullptr, s));
+                         J.dBandPhased, nb, k, J.work, J.batchStart, J.dPass, pass == 0 ? J.vis : nullptr, q));
       launches += 4;
       J.wa.inPlace = (J.tiled || pass > 0) ? 0 : 1;
       J.wa.pb.cellMin = nullptr;
       if (pass == 0 && J.cellMin) {
-        CK(rs_cell_min(J.vis, (int)J.w, (int)J.h, J.cellMin, s));
+        CK(rs_cell_min(J.vis, (int)J.w, (int)J.h, J.cellMin, q));
         launches++;
         J.wa.pb.cellMin = J.cellMin;
         J.wa.pb.cellsW = J.cellsW;
@@ -1277,6 +1353,7 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       J.wa.sparse = (pass == 0 && J.noContext && !J.tiled) ? 1 : 0;
       J.wa.nbatches = nb * k * k;
     }
+    st.join_side();
     // requests grouped by pixel layout, one launch per group per step
     std::map<std::pair<int, int>, std::vector<size_t>> groups;
     for (size_t i : act) groups[{jobs[i].dp.pb.nc, jobs[i].dp.pb.nm > 0 ? 1 : 0}].push_back(i);
