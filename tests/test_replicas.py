@@ -58,3 +58,13 @@ def test_reference_arm_only_rank0_prints(monkeypatch, capsys):
         warmup, steps, gpus = 3, 1, 2
     assert bench.run_reference_arm(Args()) is None
     assert capsys.readouterr().out == ""
+
+
+def test_term_bytes_and_ops_follow_the_unit_of_work():
+    """One neighbour term: the 4-byte corpus word, a 16-bit table read per
+    colour channel, the map byte and a 32-bit table read per map channel."""
+    import bench
+    assert bench.term_bytes(3, 0) == 10 and bench.term_ops(3, 0) == 13
+    assert bench.term_bytes(3, 1) == 15 and bench.term_ops(3, 1) == 16
+    assert bench.term_bytes(1, 0) == 6
+    assert set(bench.WAVE_DRAM_BYTES) <= {"render1024", "heal4096", "mapstyle2048", "heal256"}
