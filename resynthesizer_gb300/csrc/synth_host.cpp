@@ -370,6 +370,23 @@ struct Stream {
       CK(cudaStreamWaitEvent(s, join[i], 0));
     }
   }
+  // A thread's stream lives as long as the thread (host workers come and go
+  // with every many-request call): everything is released at thread exit.
+  // Errors are ignored (at process exit the runtime may already be gone).
+  ~Stream() {
+    for (int i = 0; i < kSide; i++) {
+      if (side[i]) cudaStreamDestroy(side[i]);
+      if (join[i]) cudaEventDestroy(join[i]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    if (s) cudaStreamDestroy(s);
+    if (hostBands) cudaFreeHost(hostBands);
+    if (hostInts) cudaFreeHost(hostInts);
+    if (hostCtr) cudaFreeHost(hostCtr);
+    if (abortHost) cudaFreeHost((void*)abortHost);
+  }
+  Stream(const Stream&) = delete;
+  Stream& operator=(const Stream&) = delete;
   Stream() {
     CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     CK(cudaHostAlloc((void**)&abortHost, sizeof(int), cudaHostAllocMapped));
