@@ -100,6 +100,9 @@ class Oracle:
         L.orc_format_from_type.argtypes = [C.POINTER(Format), C.c_int]
         L.orc_format_from_type.restype = C.c_int
         L.orc_rand_stream.argtypes = [u, u, vp]
+        L.orc_wave_engine.argtypes = [C.POINTER(Params), C.POINTER(Format), vp, u, u, vp, u, u, u, C.c_int,
+                                      C.POINTER(C.c_uint), vp]
+        L.orc_wave_engine.restype = C.c_int
 
     # -- helpers --------------------------------------------------------
     def format_indices(self, colors, mapColors, alphaT, alphaS, isMap) -> Format:
@@ -158,6 +161,20 @@ class Oracle:
         if want_state:
             return rc, tgt, st, src, hv
         return rc, tgt, st
+
+    def wave_engine(self, params: Params, fmt: Format, target: np.ndarray, corpus: np.ndarray,
+                    threads: int = 8, seed: int = 0):
+        """The GPU library's wavefront mode restated on the CPU (random orders,
+        default options): (rc, target_out, passes, betters per pass)."""
+        th, tw, _ = target.shape
+        ch, cw, _ = corpus.shape
+        tgt = np.ascontiguousarray(target, np.uint8).copy()
+        cor = np.ascontiguousarray(corpus, np.uint8)
+        passes = C.c_uint(0)
+        betters = np.zeros(6, np.uint32)
+        rc = self.lib.orc_wave_engine(C.byref(params), C.byref(fmt), _vp(tgt), tw, th, _vp(cor), cw, ch, seed,
+                                      threads, C.byref(passes), _vp(betters))
+        return rc, tgt, passes.value, betters[: passes.value].tolist()
 
     def image_synth(self, image: np.ndarray, mask: np.ndarray, fmt: int, params: Params | None,
                     mask2: np.ndarray | None = None, threads=1, cancel=0, progress=None):

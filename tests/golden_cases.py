@@ -52,3 +52,29 @@ def frozen():
         d["params"] = params_kw(z[f"{k}_params"])
         out.append(d)
     return out
+
+
+# sha256 of the target pixmap after engine() in the library's default mode
+# (wavefront, default options), with the passes run and the betters of each
+# pass.  The CPU wavefront oracle (oracle/wave_oracle.c) and the CUDA library
+# on a GB300 give these same outputs.
+WAVE_FULL = {
+    "render1024": ("710baea67bc0c8500ffee84cb1251b01baeb669d22987efcde6304f5d6489edd", 3, [1048576, 51668, 23402]),
+    "heal4096": ("1910cd1e91e8b08d462a8a5f74a1ce76df5f85f509466f2282a1bc33d7989b53", 2, [1523352, 59065]),
+    "mapstyle2048": ("45f09923a9f0f492c256d8752cf9eecb04ee2ff39533f0a7cd86c43d4a104091", 2, [4194304, 71126]),
+}
+
+
+def wave_workload(name):
+    """(target pixmap, corpus pixmap, prepareImageFormatIndices arguments, params) of a
+    full-size workload, as bench.py builds it."""
+    from resynthesizer_gb300 import workloads as W
+    if name == "render1024":
+        wl = W.render1024()
+        return wl["target"], wl["corpus"], wl["format"], wl["params"]
+    if name == "mapstyle2048":
+        wl = W.mapstyle()
+        return wl["target"], wl["corpus"], wl["format"], wl["params"]
+    wl = W.heal4096()
+    t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
+    return t, c, (3, 0, 0, 0, 0), wl["params"]

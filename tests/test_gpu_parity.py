@@ -178,6 +178,43 @@ def test_reference_entry_points_use_selected_mode():
 # --------------------------------------------------------- wavefront mode
 
 
+@pytest.mark.parametrize("name", ["render1024", "heal4096", "mapstyle2048"])
+def test_wavefront_bit_exact_full_size(name):
+    """The default mode on the full-size workloads gives exactly the output of
+    its CPU restatement (oracle/wave_oracle.c; hashes pinned in
+    golden_cases.WAVE_FULL and checked against the oracle by
+    tests/test_wave_oracle.py)."""
+    t, c, spec, kw = G.wave_workload(name)
+    r = R.engine(t, c, R.format_indices(*spec), R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
+    sha, npass, nbetter = G.WAVE_FULL[name]
+    assert r.rc == 0
+    assert r.stats["passes"] == npass and list(r.stats["betters"])[:npass] == nbetter
+    assert hashlib.sha256(r.out.tobytes()).hexdigest() == sha
+
+
+@pytest.mark.parametrize("case", ["heal", "render", "render_tiled", "mapstyle"])
+def test_wavefront_bit_exact_vs_wave_oracle(oracle, case):
+    """Small problems (corpus staged in shared memory, teams of warps per
+    target, tiling) against the CPU restatement of the wavefront mode."""
+    if case == "heal":
+        wl = W.heal_small(size=48, hole=14, ctype=1, patch=16, trys=80)
+        t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
+        spec, kw = (3, 0, 0, 0, 0), wl["params"]
+    elif case.startswith("render"):
+        wl = W.render(tile=24, out=64)
+        t, c, spec, kw = wl["target"], wl["corpus"], wl["format"], dict(wl["params"])
+        if case == "render_tiled":
+            kw.update(tileH=1, tileV=1)
+    else:
+        wl = W.mapstyle(corpus_size=40, out=64)
+        t, c, spec, kw = wl["target"], wl["corpus"], wl["format"], wl["params"]
+    r = R.engine(t, c, R.format_indices(*spec), R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
+    rc, out, passes, betters = oracle.wave_engine(make_params(**kw), oracle.format_indices(*spec), t, c)
+    assert r.rc == 0 == rc
+    assert r.stats["passes"] == passes and list(r.stats["betters"])[:passes] == betters
+    assert np.array_equal(r.out, out)
+
+
 @pytest.mark.parametrize("case", ["heal", "render", "mapstyle"])
 def test_wavefront_invariants_and_energy(oracle, case):
     if case == "heal":
