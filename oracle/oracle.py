@@ -164,8 +164,8 @@ class Oracle:
 
     def wave_engine(self, params: Params, fmt: Format, target: np.ndarray, corpus: np.ndarray,
                     threads: int = 8, seed: int = 0):
-        """The GPU library's wavefront mode restated on the CPU (random orders,
-        default options): (rc, target_out, passes, betters per pass)."""
+        """The GPU library's wavefront mode restated on the CPU (every visit
+        order, default options): (rc, target_out, passes, betters per pass)."""
         th, tw, _ = target.shape
         ch, cw, _ = corpus.shape
         tgt = np.ascontiguousarray(target, np.uint8).copy()

@@ -120,9 +120,10 @@ unsigned long long orc_energy(const orc_params *p, const orc_format *f,
 void orc_rand_stream(unsigned seed, unsigned n, int *out);
 
 /* The GPU library's wavefront mode (its default engine() path) restated on
- * the CPU, for random orders (matchContextType 0 or 1) and default options:
- * target (tw*th*total_bpp) is modified in place.  seed 0 = the library's
- * default.  Returns 0, -1 for another order, -2 for an empty target or corpus.
+ * the CPU, for every visit order and default options: target
+ * (tw*th*total_bpp) is modified in place.  seed 0 = the library's default.
+ * Returns 0, -1 for a matchContextType outside 0..8, -2 for an empty target
+ * or corpus.
  * passesOut and bettersOut (6 entries) may be NULL.  (wave_oracle.c) */
 int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *target, unsigned tw, unsigned th,
                     const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,

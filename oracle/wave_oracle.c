@@ -5,16 +5,18 @@
  * library's default mode, loaded by tests/ and never by the product.
  *
  * The wavefront mode is a deterministic schedule, so it can be restated
- * exactly.  For random visit orders (matchContextType 0 and 1):
+ * exactly (every visit order, matchContextType 0..8):
  *   - targets (selected pixels) and corpus points (mask 0xFF, opaque) in
  *     row-major order; hasValue = context (matchContextType != 0, unselected,
  *     opaque), sourceOf = (-1, -1)  (lib/engine.c:338-431 semantics);
- *   - passes over prefixes [n, n, 3n/4, ...] of one random order (rank = a
- *     hash of the pixel), stopping when betters < n/10 after at least
- *     minPasses (lib/refiner.h:42-122, lib/passes.h:67-93);
+ *   - passes over prefixes [n, n, 3n/4, ...] of one visit order (random
+ *     orders: rank = a hash of the pixel; directional orders: the reference's
+ *     order), stopping when betters < n/10 after at least minPasses
+ *     (lib/refiner.h:42-122, lib/passes.h:67-93);
  *   - a pass is a sequence of batches: pass 0 cuts the ranks into bands of
- *     16, 32, 64, ... targets, later passes use one band, and every band is
- *     split into k x k colour phases by (x mod k, y mod k);
+ *     16, 32, 64, ... targets (random orders) or of equal widths of at least
+ *     1024 (directional), later passes use one band, and every band is split
+ *     into k x k colour phases by (x mod k, y mod k);
  *   - within a batch, targets see the state left by earlier batches only
  *     (visit stamps in pass 0, staged stores in later passes);
  *   - a target's patch is itself plus the nearest sorted offsets (radius
@@ -247,7 +249,8 @@ static int phase_side(const wpt *offs, int noffs, int limit, int w, int h) {
 int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *target, unsigned tw, unsigned th,
                     const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,
                     unsigned *passesOut, unsigned *bettersOut) {
-  if (p->matchContextType != 0 && p->matchContextType != 1) return -1;
+  if (p->matchContextType < 0 || p->matchContextType > 8) return -1;
+  const int randomOrder = p->matchContextType <= 1;
   const size_t tn = (size_t)tw * th, cn = (size_t)cw * ch;
   const int bpp = f->total_bpp;
   wave w;
@@ -386,12 +389,24 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
         m = m * 3 / 4;
       }
     }
-    /* one random order for every pass: rank = hash of the pixel */
+    /* one visit order for every pass: random orders rank a target by a hash
+     * of its pixel; the directional orders are the reference's own order
+     * (lib/orderTarget.h:268-343) and rank a target by its position in it */
     const uint32_t orderSeed = w.seed ^ 0x5bd1e995u;
     int *rank = malloc((size_t)n * sizeof *rank);
-    for (int t = 0; t < n; t++)
-      rank[t] = (int)umulhi32(mix32((uint32_t)(targets[t].y * (int)tw + targets[t].x) * 0x9E3779B1u ^ orderSeed),
-                              (uint32_t)n);
+    if (randomOrder) {
+      for (int t = 0; t < n; t++)
+        rank[t] = (int)umulhi32(mix32((uint32_t)(targets[t].y * (int)tw + targets[t].x) * 0x9E3779B1u ^ orderSeed),
+                                (uint32_t)n);
+    } else {
+      if (orc_order_targets(p->matchContextType, (orc_pt *)targets, (unsigned)n)) {
+        free(rank);
+        free(offs);
+        rc = -1;
+        goto done;
+      }
+      for (int t = 0; t < n; t++) rank[t] = t;
+    }
     int *key = malloc((size_t)n * sizeof *key);
     wpt *bucket = malloc((size_t)n * sizeof *bucket);
     int *start = malloc(((size_t)WO_MAX_BANDS * k * k + 1) * sizeof *start);
@@ -401,11 +416,13 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
       const unsigned end = ends[pass];
       int bandEnds[WO_MAX_BANDS], nb = 0;
       if (pass == 0) {
-        double size = 16, b = 0;
+        /* random orders: 16, 32, 64, ...; directional: equal widths of at
+         * least 1024 */
+        double size = randomOrder ? 16.0 : fmax(1024.0, ceil((double)end / WO_MAX_BANDS)), b = 0;
         while (b < end && nb < WO_MAX_BANDS - 1) {
           b = fmin((double)end, b + fmax(1.0, size));
           bandEnds[nb++] = (int)b;
-          size *= 2.0;
+          if (randomOrder) size *= 2.0;
         }
         if (bandEnds[nb - 1] < (int)end) bandEnds[nb++] = (int)end;
       } else {

@@ -49,8 +49,23 @@ def test_wave_oracle_threads_and_invariants(oracle, threads):
     assert 1 <= passes <= 6 and betters[0] == int(sel.sum())
 
 
-def test_wave_oracle_rejects_directional_orders(oracle):
-    wl = W.heal_small(size=24, hole=8, ctype=2, patch=9, trys=20)
+@pytest.mark.parametrize("ctype", [2, 5, 8])
+def test_wave_oracle_directional_orders(oracle, ctype):
+    """Directional orders (the reference's own visit order, bands of equal
+    width): deterministic, and the same invariants."""
+    wl = W.heal_small(size=40, hole=12, ctype=ctype, patch=16, trys=40, index=ctype)
     t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
-    rc, _, _, _ = oracle.wave_engine(make_params(**wl["params"]), oracle.format_indices(3, 0, 0, 0, 0), t, c)
+    p, fmt = make_params(**wl["params"]), oracle.format_indices(3, 0, 0, 0, 0)
+    rc, out, passes, betters = oracle.wave_engine(p, fmt, t, c, threads=1)
+    rc2, out2, _, _ = oracle.wave_engine(p, fmt, t, c, threads=4)
+    assert rc == rc2 == 0 and np.array_equal(out, out2)
+    sel = t[..., 0] != 0
+    assert np.array_equal(out[~sel], t[~sel]) and betters[0] == int(sel.sum())
+
+
+def test_wave_oracle_rejects_unknown_order(oracle):
+    wl = W.heal_small(size=24, hole=8, ctype=1, patch=9, trys=20)
+    t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
+    rc, _, _, _ = oracle.wave_engine(make_params(**dict(wl["params"], matchContextType=9)),
+                                     oracle.format_indices(3, 0, 0, 0, 0), t, c)
     assert rc == -1
