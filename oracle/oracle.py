@@ -51,6 +51,12 @@ class Stats(C.Structure):
 PROGRESS = C.CFUNCTYPE(None, C.c_int, C.c_void_p)
 
 
+class WaveOpts(C.Structure):
+    """orc_wave_opts: the wavefront schedule options (0 = default)."""
+    _fields_ = [("firstBatch", C.c_uint), ("bandGrowth", C.c_uint), ("phaseSide", C.c_uint),
+                ("minPasses", C.c_uint)]
+
+
 def make_params(tileH=0, tileV=0, matchContextType=1, mapWeight=0.5, sensitivity=0.117,
                 patchSize=30, maxProbeCount=200) -> Params:
     return Params(tileH, tileV, matchContextType, mapWeight, sensitivity, patchSize, maxProbeCount)
@@ -103,6 +109,9 @@ class Oracle:
         L.orc_wave_engine.argtypes = [C.POINTER(Params), C.POINTER(Format), vp, u, u, vp, u, u, u, C.c_int,
                                       C.POINTER(C.c_uint), vp]
         L.orc_wave_engine.restype = C.c_int
+        L.orc_wave_engine_ex.argtypes = [C.POINTER(Params), C.POINTER(Format), vp, u, u, vp, u, u, u, C.c_int,
+                                         C.POINTER(WaveOpts), C.POINTER(C.c_uint), vp, vp, vp, C.POINTER(C.c_uint)]
+        L.orc_wave_engine_ex.restype = C.c_int
 
     # -- helpers --------------------------------------------------------
     def format_indices(self, colors, mapColors, alphaT, alphaS, isMap) -> Format:
@@ -175,6 +184,25 @@ class Oracle:
         rc = self.lib.orc_wave_engine(C.byref(params), C.byref(fmt), _vp(tgt), tw, th, _vp(cor), cw, ch, seed,
                                       threads, C.byref(passes), _vp(betters))
         return rc, tgt, passes.value, betters[: passes.value].tolist()
+
+    def wave_engine_state(self, params: Params, fmt: Format, target: np.ndarray, corpus: np.ndarray,
+                          threads: int = 8, seed: int = 0, **schedule):
+        """wave_engine with schedule options (firstBatch, bandGrowth, phaseSide,
+        minPasses) and the final state: (rc, target_out, passes, betters,
+        sourceOf (H, W, 2), hasValue (H, W), batches)."""
+        th, tw, _ = target.shape
+        ch, cw, _ = corpus.shape
+        tgt = np.ascontiguousarray(target, np.uint8).copy()
+        cor = np.ascontiguousarray(corpus, np.uint8)
+        passes, batches = C.c_uint(0), C.c_uint(0)
+        betters = np.zeros(6, np.uint32)
+        src = np.zeros((th, tw, 2), np.int32)
+        hv = np.zeros((th, tw), np.uint8)
+        opts = WaveOpts(**schedule)
+        rc = self.lib.orc_wave_engine_ex(C.byref(params), C.byref(fmt), _vp(tgt), tw, th, _vp(cor), cw, ch, seed,
+                                         threads, C.byref(opts), C.byref(passes), _vp(betters), _vp(src), _vp(hv),
+                                         C.byref(batches))
+        return rc, tgt, passes.value, betters[: passes.value].tolist(), src, hv, batches.value
 
     def image_synth(self, image: np.ndarray, mask: np.ndarray, fmt: int, params: Params | None,
                     mask2: np.ndarray | None = None, threads=1, cancel=0, progress=None):

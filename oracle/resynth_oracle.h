@@ -129,6 +129,20 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
                     const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,
                     unsigned *passesOut, unsigned *bettersOut);
 
+/* Schedule options of the wavefront mode (TResynthOptions' firstBatch,
+ * bandGrowth, phaseSide, minPasses; 0 = the library's default). */
+typedef struct {
+  unsigned int firstBatch, bandGrowth, phaseSide, minPasses;
+} orc_wave_opts;
+
+/* orc_wave_engine with schedule options (opt may be NULL) and optional
+ * outputs: the final sourceOf and hasValue (tw*th each) and the number of
+ * non-empty batches run. */
+int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *target, unsigned tw, unsigned th,
+                       const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,
+                       const orc_wave_opts *opt, unsigned *passesOut, unsigned *bettersOut, orc_pt *sourceOut,
+                       unsigned char *hasValueOut, unsigned *batchesOut);
+
 #ifdef __cplusplus
 }
 #endif

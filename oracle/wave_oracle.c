@@ -246,9 +246,12 @@ static int phase_side(const wpt *offs, int noffs, int limit, int w, int h) {
  * in its default mode), random orders only.  target is modified in place
  * (colours).  Returns 0, or -1 for an unsupported order.  passesOut and
  * bettersOut (WO_PASSES entries) may be NULL. */
-int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *target, unsigned tw, unsigned th,
-                    const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,
-                    unsigned *passesOut, unsigned *bettersOut) {
+int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *target, unsigned tw, unsigned th,
+                       const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,
+                       const orc_wave_opts *opt, unsigned *passesOut, unsigned *bettersOut, orc_pt *sourceOut,
+                       unsigned char *hasValueOut, unsigned *batchesOut) {
+  static const orc_wave_opts defaults = {0, 0, 0, 0};
+  if (!opt) opt = &defaults;
   if (p->matchContextType < 0 || p->matchContextType > 8) return -1;
   const int randomOrder = p->matchContextType <= 1;
   const size_t tn = (size_t)tw * th, cn = (size_t)cw * ch;
@@ -374,12 +377,12 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
     free(keys);
     w.offs = offs;
     w.noffs = noffs;
-    const int k = phase_side(offs, (int)nall, w.limit, w.boxW, w.boxH);
+    const int k = opt->phaseSide ? (int)opt->phaseSide : phase_side(offs, (int)nall, w.limit, w.boxW, w.boxH);
     /* corpus staged in shared memory when it fits: then probes stay per pixel */
     const size_t padWords = (((size_t)(cw + 12) * (ch + 12)) + 3) & ~(size_t)3;
     const size_t smem = 2064 + padWords * 4 * (w.nm ? 2 : 1) + 16 * 2048;
     w.probeShare = (smem > WO_STAGED_LIMIT && n >= 131072) ? 1 : 0;
-    const int minPasses = (!context && w.nm == 0) ? 3 : 0;
+    const int minPasses = opt->minPasses ? (int)opt->minPasses : ((!context && w.nm == 0) ? 3 : 0);
     unsigned ends[WO_PASSES];
     {
       unsigned m = (unsigned)n;
@@ -418,11 +421,13 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
       if (pass == 0) {
         /* random orders: 16, 32, 64, ...; directional: equal widths of at
          * least 1024 */
-        double size = randomOrder ? 16.0 : fmax(1024.0, ceil((double)end / WO_MAX_BANDS)), b = 0;
+        const double first = opt->firstBatch ? opt->firstBatch : (randomOrder ? 16.0 : 1024.0);
+        const double growth = (opt->bandGrowth ? opt->bandGrowth : 200u) / 100.0;
+        double size = randomOrder ? first : fmax(first, ceil((double)end / WO_MAX_BANDS)), b = 0;
         while (b < end && nb < WO_MAX_BANDS - 1) {
           b = fmin((double)end, b + fmax(1.0, size));
           bandEnds[nb++] = (int)b;
-          if (randomOrder) size *= 2.0;
+          if (randomOrder) size *= growth;
         }
         if (bandEnds[nb - 1] < (int)end) bandEnds[nb++] = (int)end;
       } else {
@@ -454,6 +459,7 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
         w.batch = bucket + start[b];
         w.nslots = start[b + 1] - start[b];
         if (!w.nslots) continue;
+        if (batchesOut) (*batchesOut)++;
         w.batchIdx = b;
         w.visCur = pass == 0 ? b : 0x7ffffffe;
         run_batch(&w, nthreads);
@@ -472,6 +478,13 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
       if ((double)((float)betters / (float)n) < 0.1 && pass + 1 >= minPasses) break;   /* lib/refiner.h:111 */
     }
     if (passesOut) *passesOut = passes;
+    if (sourceOut)
+      for (size_t i = 0; i < tn; i++) {
+        sourceOut[i].x = src[i].x;
+        sourceOut[i].y = src[i].y;
+      }
+    if (hasValueOut)
+      for (size_t i = 0; i < tn; i++) hasValueOut[i] = vis[i] != 0x7fffffff;
     (void)bettersTotal;
     free(rank);
     free(key);
@@ -493,4 +506,11 @@ done:
   free(vis);
   free(src);
   return rc;
+}
+
+int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *target, unsigned tw, unsigned th,
+                    const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,
+                    unsigned *passesOut, unsigned *bettersOut) {
+  return orc_wave_engine_ex(p, f, target, tw, th, corpus, cw, ch, seed, nthreads, NULL, passesOut, bettersOut, NULL,
+                            NULL, NULL);
 }
