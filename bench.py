@@ -175,6 +175,26 @@ def cpu_sample(threads: int, side: int = SAMPLE_SIDE):
                 sample=f"{side}x{side} target from the same 128x128 tile (P=16, trys=300), one run")
 
 
+def cpu_same_schedule(target, corpus, spec, params: dict, gpu_out, threads: int):
+    """The wavefront schedule itself on the CPU: its plain-C restatement
+    (oracle/wave_oracle.c) on the whole workload with `threads` threads, and
+    whether it gives the GPU's output byte for byte.  Separates what the
+    schedule gains over the reference's sequential engine from what the GPU
+    gains over the same schedule on CPU cores."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    o = O.Oracle()
+    fmt = o.format_indices(*spec)
+    t0 = time.perf_counter()
+    rc, out, passes, _ = o.wave_engine(O.make_params(**params), fmt, target, corpus, threads=threads)
+    dt = time.perf_counter() - t0
+    px = int((target[..., 0] != 0).sum())
+    return {"value": px / dt, "unit": "target px/s", "cores": threads, "seconds": dt, "passes": passes,
+            "identical_to_gpu": bool(rc == 0 and np.array_equal(out, gpu_out)),
+            "what": "the wavefront schedule restated in C (oracle/wave_oracle.c), whole workload"}
+
+
 def load_workload(name: str):
     """(name, target pixmap, corpus pixmap, prepareImageFormatIndices args, params) of a workload."""
     from resynthesizer_gb300 import workloads as W
@@ -567,6 +587,11 @@ def main():
         stt = cpu_sample(threads=1)
         line["cpu_baseline"] = {"value": mt["value"], "unit": "target px/s", "cores": 8, "kind": mt["kind"],
                                 "sample": mt["sample"], "single_thread_value": stt["value"]}
+        try:
+            line["cpu_same_schedule"] = cpu_same_schedule(wl["target"], wl["corpus"], wl["format"], wl["params"],
+                                                          res.out, min(16, os.cpu_count() or 1))
+        except Exception as e:   # an informative extra: never fails the bench line
+            line["cpu_same_schedule"] = {"error": repr(e)[:200]}
     if not args.no_learned and wname == "render1024" and rank == 0:
         # learned vs plain (outside every timed region above): a 1024^2 heal,
         # network trained on pairs from four plain runs, 200 probes each way
