@@ -11,9 +11,10 @@
 // Kernels:
 //   k_replay   one CTA visiting targets in the reference order (bit-exact
 //              sequential replay of lib/synthesize.h:426-642)
-//   k_wave     warp-per-target synthesis of one wavefront batch
+//   k_wave     one wavefront batch: a warp (or a team of warps) per target
+//   k_wave_multi  step b of many requests at once (batch b of every request)
 //   k_commit   applies a batch's staged results when they cannot be stored in
-//              place (tiled targets)
+//              place (refinement passes, tiled targets)
 //   k_frozen   frozen-state best fit over explicit candidate lists
 //   k_energy   full-patch metric at each target's source
 #include <climits>
