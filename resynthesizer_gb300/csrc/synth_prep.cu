@@ -307,9 +307,6 @@ extern "C" cudaError_t rs_prep_corpus(const uint8_t* raw, int w, int h, int bpp,
 extern "C" int rs_prep_scratch_ints(int w, int h) { return 2 * blocks_for(w * h, kChunk) + 1; }
 
 // Buckets the targets of one pass into batches: out[batchStart[b] ..
-// batchStart[b+1]) are the targets of batch b = band * k * k + phase.
-// work: 3 * nkeys + 1 + n ints.
-// Buckets the targets of one pass into batches: out[batchStart[b] ..
 // batchStart[b+1]) are the targets of batch b = band * k * k + phase, in the
 // order of the target list.  work: rs_prep_batches_ints(n, nkeys) ints.
 extern "C" cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int randomOrder,
