@@ -78,3 +78,32 @@ def wave_workload(name):
     wl = W.heal4096()
     t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
     return t, c, (3, 0, 0, 0, 0), wl["params"]
+
+
+# Small wavefront cases (corpus staged in shared memory, teams of warps per
+# target, tiling, maps): output hash, passes, betters per pass.  The CUDA
+# library and the CPU wavefront oracle give these same outputs.
+WAVE_SMALL = {
+    "heal": ("c242d24b4fd897e0f3b05f1f20d2c53a1b2334934f660664a5eb2ae4230e2eed", 3, [196, 39, 5]),
+    "render": ("ab1318035955c00230beda01b7983e6105570027b8bdc5d8e9dc027a666a06ef", 3, [4096, 558, 217]),
+    "render_tiled": ("3fedb93d5756a96d6ca9558a2285e458ab9a3cd3d148a05d755a976f38c985a0", 3, [4096, 762, 313]),
+    "mapstyle": ("784df1c59b1ed927bf680c27d91aeea78723242469524e590d968b3a0786da33", 2, [4096, 315]),
+}
+
+
+def wave_small_case(case):
+    """(target pixmap, corpus pixmap, prepareImageFormatIndices arguments, params) of a small
+    wavefront case."""
+    from resynthesizer_gb300 import workloads as W
+    if case == "heal":
+        wl = W.heal_small(size=48, hole=14, ctype=1, patch=16, trys=80)
+        t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
+        return t, c, (3, 0, 0, 0, 0), wl["params"]
+    if case.startswith("render"):
+        wl = W.render(tile=24, out=64)
+        kw = dict(wl["params"])
+        if case == "render_tiled":
+            kw.update(tileH=1, tileV=1)
+        return wl["target"], wl["corpus"], wl["format"], kw
+    wl = W.mapstyle(corpus_size=40, out=64)
+    return wl["target"], wl["corpus"], wl["format"], wl["params"]

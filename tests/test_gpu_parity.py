@@ -196,18 +196,7 @@ def test_wavefront_bit_exact_full_size(name):
 def test_wavefront_bit_exact_vs_wave_oracle(oracle, case):
     """Small problems (corpus staged in shared memory, teams of warps per
     target, tiling) against the CPU restatement of the wavefront mode."""
-    if case == "heal":
-        wl = W.heal_small(size=48, hole=14, ctype=1, patch=16, trys=80)
-        t, c = W.simple_to_pixmaps(wl["image"], wl["mask"])
-        spec, kw = (3, 0, 0, 0, 0), wl["params"]
-    elif case.startswith("render"):
-        wl = W.render(tile=24, out=64)
-        t, c, spec, kw = wl["target"], wl["corpus"], wl["format"], dict(wl["params"])
-        if case == "render_tiled":
-            kw.update(tileH=1, tileV=1)
-    else:
-        wl = W.mapstyle(corpus_size=40, out=64)
-        t, c, spec, kw = wl["target"], wl["corpus"], wl["format"], wl["params"]
+    t, c, spec, kw = G.wave_small_case(case)
     r = R.engine(t, c, R.format_indices(*spec), R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
     rc, out, passes, betters = oracle.wave_engine(make_params(**kw), oracle.format_indices(*spec), t, c)
     assert r.rc == 0 == rc

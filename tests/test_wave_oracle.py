@@ -32,6 +32,15 @@ def test_wave_oracle_full_size_pinned(oracle, name):
     assert hashlib.sha256(out.tobytes()).hexdigest() == sha
 
 
+@pytest.mark.parametrize("case", sorted(G.WAVE_SMALL))
+def test_wave_oracle_small_cases_pinned(oracle, case):
+    t, c, spec, kw = G.wave_small_case(case)
+    rc, out, passes, betters = oracle.wave_engine(make_params(**kw), oracle.format_indices(*spec), t, c)
+    sha, npass, nbetter = G.WAVE_SMALL[case]
+    assert rc == 0 and (passes, betters) == (npass, nbetter)
+    assert hashlib.sha256(out.tobytes()).hexdigest() == sha
+
+
 @pytest.mark.parametrize("threads", [1, 3])
 def test_wave_oracle_threads_and_invariants(oracle, threads):
     """Same output for any thread count; only target colours change, and every
