@@ -54,7 +54,7 @@ PROGRESS = C.CFUNCTYPE(None, C.c_int, C.c_void_p)
 class WaveOpts(C.Structure):
     """orc_wave_opts: the wavefront schedule options (0 = default)."""
     _fields_ = [("firstBatch", C.c_uint), ("bandGrowth", C.c_uint), ("phaseSide", C.c_uint),
-                ("minPasses", C.c_uint)]
+                ("minPasses", C.c_uint), ("probeShare", C.c_uint)]
 
 
 def make_params(tileH=0, tileV=0, matchContextType=1, mapWeight=0.5, sensitivity=0.117,

@@ -133,6 +133,7 @@ int orc_wave_engine(const orc_params *p, const orc_format *f, unsigned char *tar
  * bandGrowth, phaseSide, minPasses; 0 = the library's default). */
 typedef struct {
   unsigned int firstBatch, bandGrowth, phaseSide, minPasses;
+  unsigned int probeShare;   /* 0: the library's rule, 1: always share probes by slot group, 2: never */
 } orc_wave_opts;
 
 /* orc_wave_engine with schedule options (opt may be NULL) and optional

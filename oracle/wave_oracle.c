@@ -250,7 +250,7 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
                        const unsigned char *corpus, unsigned cw, unsigned ch, unsigned seed, int nthreads,
                        const orc_wave_opts *opt, unsigned *passesOut, unsigned *bettersOut, orc_pt *sourceOut,
                        unsigned char *hasValueOut, unsigned *batchesOut) {
-  static const orc_wave_opts defaults = {0, 0, 0, 0};
+  static const orc_wave_opts defaults = {0, 0, 0, 0, 0};
   if (!opt) opt = &defaults;
   if (p->matchContextType < 0 || p->matchContextType > 8) return -1;
   const int randomOrder = p->matchContextType <= 1;
@@ -381,7 +381,7 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
     /* corpus staged in shared memory when it fits: then probes stay per pixel */
     const size_t padWords = (((size_t)(cw + 12) * (ch + 12)) + 3) & ~(size_t)3;
     const size_t smem = 2064 + padWords * 4 * (w.nm ? 2 : 1) + 16 * 2048;
-    w.probeShare = (smem > WO_STAGED_LIMIT && n >= 131072) ? 1 : 0;
+    w.probeShare = opt->probeShare == 1 ? 1 : opt->probeShare == 2 ? 0 : (smem > WO_STAGED_LIMIT && n >= 131072) ? 1 : 0;
     const int minPasses = opt->minPasses ? (int)opt->minPasses : ((!context && w.nm == 0) ? 3 : 0);
     unsigned ends[WO_PASSES];
     {
