@@ -112,6 +112,9 @@ class Oracle:
         L.orc_wave_engine_ex.argtypes = [C.POINTER(Params), C.POINTER(Format), vp, u, u, vp, u, u, u, C.c_int,
                                          C.POINTER(WaveOpts), C.POINTER(C.c_uint), vp, vp, vp, C.POINTER(C.c_uint)]
         L.orc_wave_engine_ex.restype = C.c_int
+        L.orc_wave_image_synth.argtypes = [C.POINTER(ImageBuffer), C.POINTER(ImageBuffer), C.POINTER(ImageBuffer),
+                                           C.c_int, C.POINTER(Params), u, C.c_int]
+        L.orc_wave_image_synth.restype = C.c_int
 
     # -- helpers --------------------------------------------------------
     def format_indices(self, colors, mapColors, alphaT, alphaS, isMap) -> Format:
@@ -225,6 +228,24 @@ class Oracle:
                                       C.cast(cb, C.c_void_p) if cb else None, None, C.byref(cf),
                                       C.byref(st))
         return rc, img, st
+
+    def wave_image_synth(self, image: np.ndarray, mask: np.ndarray, fmt: int, params: Params | None,
+                         mask2: np.ndarray | None = None, threads: int = 8, seed: int = 0):
+        """The Simple API around the wavefront restatement (what the GPU
+        library's imageSynth gives in wavefront mode): (rc, image_out)."""
+        img = np.ascontiguousarray(image, np.uint8).copy()
+        h, w = img.shape[:2]
+        bpp = img.shape[2] if img.ndim == 3 else 1
+        ib = ImageBuffer(_u8p(img), w, h, w * bpp)
+        m = np.ascontiguousarray(mask, np.uint8)
+        mb = ImageBuffer(_u8p(m), m.shape[1], m.shape[0], m.shape[1])
+        m2 = None
+        if mask2 is not None:
+            m2a = np.ascontiguousarray(mask2, np.uint8)
+            m2 = ImageBuffer(_u8p(m2a), m2a.shape[1], m2a.shape[0], m2a.shape[1])
+        rc = self.lib.orc_wave_image_synth(C.byref(ib), C.byref(mb), C.byref(m2) if m2 else None, fmt,
+                                           C.byref(params) if params is not None else None, seed, threads)
+        return rc, img
 
     def frozen(self, params, fmt, target, corpus, hasValue, sourceOf, targets, candStart, cands):
         th, tw, _ = target.shape

@@ -524,11 +524,40 @@ done_targets:
 
 /* ------------------------------------------------------------ simple API */
 
-int orc_image_synth(orc_image_buffer *img, orc_image_buffer *mask, orc_image_buffer *mask2,
-                    int fmt, const orc_params *p, int nthreads,
-                    void (*progress)(int, void *), void *ctx, int *cancel, orc_stats *stats) {
-  int zero = 0;
-  if (!cancel) cancel = &zero;
+/* The engine behind a Simple API call: the reference engine (nthreads >= 1)
+ * or the GPU library's wavefront mode restated (wave != 0, wave_oracle.c). */
+typedef struct {
+  int wave, nthreads;
+  unsigned seed;
+  void (*progress)(int, void *);
+  void *ctx;
+  int *cancel;
+  orc_stats *stats;
+} simple_engine;
+
+static int run_simple_engine(const simple_engine *se, const orc_params *p, const orc_format *f,
+                             unsigned char *tgt, unsigned w, unsigned h, const unsigned char *cor) {
+  if (!se->wave)
+    return orc_engine(p, f, tgt, w, h, cor, w, h, se->nthreads, se->progress, se->ctx, se->cancel, se->stats,
+                      NULL, NULL);
+  if (p->patchSize > MAX_NEIGHBORS) return ERR_PATCH_SIZE;                   /* engine.c:591 */
+  const int rc = orc_wave_engine(p, f, tgt, w, h, cor, w, h, se->seed, se->nthreads, NULL, NULL);
+  if (rc == -1) return ERR_CONTEXT_TYPE;
+  if (rc == -2) {                                                           /* engine.c:605-627 */
+    for (size_t i = 0; i < (size_t)w * h; i++)
+      if (tgt[i * f->total_bpp]) return ERR_EMPTY_CORPUS;
+    return ERR_EMPTY_TARGET;
+  }
+  return rc;
+}
+
+/* lib/imageSynth.c:61-216 with adaptSimpleAPI / antiAdaptImage
+ * (lib/adaptSimple.h:47-354): the caller's row-padded image becomes two
+ * unpadded pixmaps with the mask interleaved first (the corpus takes mask2,
+ * or the inverted mask); the engine's colours go back into the caller's
+ * buffer only on success and without cancellation. */
+static int simple_api(orc_image_buffer *img, orc_image_buffer *mask, orc_image_buffer *mask2, int fmt,
+                      const orc_params *p, const simple_engine *se) {
   if (img->width != mask->width || img->height != mask->height) return ERR_MASK_MISMATCH;
   orc_params defaults = {0, 0, 1, 0.5, 0.117, 30, 200};    /* lib/engineParams.c:8-19 */
   if (!p) p = &defaults;
@@ -549,8 +578,8 @@ int orc_image_synth(orc_image_buffer *img, orc_image_buffer *mask, orc_image_buf
       memcpy(tgt + d + 1, s, bpp);
       memcpy(cor + d + 1, s, bpp);
     }
-  rc = orc_engine(p, &f, tgt, w, h, cor, w, h, nthreads, progress, ctx, cancel, stats, NULL, NULL);
-  if (!rc && !*cancel)
+  rc = run_simple_engine(se, p, &f, tgt, w, h, cor);
+  if (!rc && !*se->cancel)
     for (unsigned y = 0; y < h; y++)
       for (unsigned x = 0; x < w; x++)
         memcpy(img->data + y * img->rowBytes + (size_t)x * bpp,
@@ -558,6 +587,21 @@ int orc_image_synth(orc_image_buffer *img, orc_image_buffer *mask, orc_image_buf
   free(tgt);
   free(cor);
   return rc;
+}
+
+int orc_image_synth(orc_image_buffer *img, orc_image_buffer *mask, orc_image_buffer *mask2,
+                    int fmt, const orc_params *p, int nthreads,
+                    void (*progress)(int, void *), void *ctx, int *cancel, orc_stats *stats) {
+  int zero = 0;
+  simple_engine se = {0, nthreads, 0, progress, ctx, cancel ? cancel : &zero, stats};
+  return simple_api(img, mask, mask2, fmt, p, &se);
+}
+
+int orc_wave_image_synth(orc_image_buffer *img, orc_image_buffer *mask, orc_image_buffer *mask2, int fmt,
+                         const orc_params *p, unsigned seed, int nthreads) {
+  int zero = 0;
+  simple_engine se = {1, nthreads, seed, NULL, NULL, &zero, NULL};
+  return simple_api(img, mask, mask2, fmt, p, &se);
 }
 
 /* ---------------------------------------------------- frozen and energy */

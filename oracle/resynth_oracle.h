@@ -144,6 +144,13 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
                        const orc_wave_opts *opt, unsigned *passesOut, unsigned *bettersOut, orc_pt *sourceOut,
                        unsigned char *hasValueOut, unsigned *batchesOut);
 
+/* The Simple API (lib/imageSynth.c:61-216, the reference's adapters) around
+ * the wavefront restatement: what the GPU library's imageSynth / imageSynth2
+ * give in wavefront mode.  mask2 NULL = imageSynth.  Returns the reference's
+ * error codes. */
+int orc_wave_image_synth(orc_image_buffer *img, orc_image_buffer *mask, orc_image_buffer *mask2, int imageFormat,
+                         const orc_params *p, unsigned seed, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -220,17 +220,37 @@ class Result:
     has_value: np.ndarray | None = None
 
 
+def _padded(a: np.ndarray, pad: int):
+    """(row-padded copy, ImageBuffer over it): each row of `a` followed by
+    `pad` bytes of 0xA5, as a caller's buffer with rowBytes > width * bpp."""
+    h, w = a.shape[:2]
+    bpp = a.shape[2] if a.ndim == 3 else 1
+    buf = np.full((h, w * bpp + pad), 0xA5, np.uint8)
+    buf[:, :w * bpp] = a.reshape(h, w * bpp)
+    return buf, ImageBuffer(buf.ctypes.data_as(C.POINTER(C.c_ubyte)), w, h, w * bpp + pad)
+
+
 def image_synth(image, mask, fmt, p: ImageSynthParameters | None = None, mask2=None, opts: Options | None = None,
-                cancel=0, progress=None, raw_entry=False) -> Result:
+                cancel=0, progress=None, raw_entry=False, row_pad: int = 0) -> Result:
     """Simple API on an (H, W, bpp) image and (H, W) mask.  raw_entry=True
-    calls the reference-named imageSynth/imageSynth2 entry point itself."""
+    calls the reference-named imageSynth/imageSynth2 entry point itself.
+    row_pad > 0 hands the library row-padded buffers (rowBytes = width * bpp
+    + row_pad); the result is then checked to leave the padding untouched."""
     img = np.ascontiguousarray(image, np.uint8).copy()
     m = np.ascontiguousarray(mask, np.uint8)
     ib, mb = _buf(img), _buf(m)
+    padded = None
+    if row_pad:
+        pimg, ib = _padded(img, row_pad)
+        pm, mb = _padded(m, row_pad)
+        padded = (pimg, pm)
     m2 = None
     if mask2 is not None:
         m2a = np.ascontiguousarray(mask2, np.uint8)
         m2 = _buf(m2a)
+        if row_pad:
+            pm2, m2 = _padded(m2a, row_pad)
+            padded = padded + (pm2,)
     cf = C.c_int(cancel)
     cb = PROGRESS(progress) if progress else None
     cbp = C.cast(cb, C.c_void_p) if cb else None
@@ -244,6 +264,12 @@ def image_synth(image, mask, fmt, p: ImageSynthParameters | None = None, mask2=N
     else:
         rc = lib().imageSynthEx(C.byref(ib), C.byref(mb), C.byref(m2) if m2 else None, fmt, pp, cbp, None,
                                 C.byref(cf), C.byref(opts) if opts else None, C.byref(st))
+    if padded is not None:
+        h, w = m.shape
+        rowb = img.size // h
+        if not (padded[0][:, rowb:] == 0xA5).all():
+            raise RuntimeError("the library wrote into the row padding of the image buffer")
+        img = np.ascontiguousarray(padded[0][:, :rowb]).reshape(img.shape)
     r = Result(rc, img, st.as_dict())
     if opts is not None and opts.recordState and rc == 0:
         h, w = m.shape

@@ -540,9 +540,14 @@ int default_mode() {
   return g_defaultMode;
 }
 
+// Layouts the kernels handle, with every byte they read (colours, map
+// channels, alpha) inside the pixel: a TFormatIndices that points past
+// total_bpp would make the device read past the end of the caller's buffers.
 bool supported_format(const TFormatIndices& f) {
   return f.img_match_bpp >= 1 && f.img_match_bpp <= 3 && f.map_match_bpp <= 3 && f.total_bpp <= 8 &&
-         f.colorEndBip == 1 + f.img_match_bpp;
+         f.colorEndBip == 1 + f.img_match_bpp && f.colorEndBip <= f.total_bpp &&
+         (!f.map_match_bpp || f.map_start_bip + f.map_match_bpp <= f.total_bpp) &&
+         ((!f.isAlphaTarget && !f.isAlphaSource) || f.alpha_bip < f.total_bpp);
 }
 
 // Device problem built from device pixmaps.

@@ -1529,19 +1529,69 @@ constexpr size_t kNoAllocScratchBytes = 8u << 20;   // 8 MiB
 constexpr size_t kNoAllocTableBytes = 2 * kTable * sizeof(uint32_t);
 static __device__ __align__(256) unsigned char g_noAllocScratch[kNoAllocScratchBytes];
 
-// Point k (0 <= k < 8r) of the square ring at Chebyshev distance r >= 1.
-__device__ __forceinline__ void ring_point(int r, int k, int& dx, int& dy) {
-  const int side = k / (2 * r), t = k % (2 * r);
-  if (side == 0) { dx = -r + t; dy = -r; }
-  else if (side == 1) { dx = r; dy = -r + t; }
-  else if (side == 2) { dx = r - t; dy = r; }
-  else { dx = -r; dy = r - t; }
+// Ring keys: (dx^2 + dy^2) << kRingIdxBits | (kRingIdxMask - box position).
+// An accepted problem holds its target and corpus words in the working array,
+// so the offset box (the smaller of the two images on each axis) has at most
+// kMaxBoxPx pixels: its (2bw - 1)(2bh - 1) positions fit in kRingIdxBits and
+// dx^2 + dy^2 < kMaxBoxPx^2 < 2^40, so the key fits 64 bits.
+constexpr size_t kMaxBoxPx = (kNoAllocScratchBytes - kNoAllocTableBytes) / 4 / 2;
+constexpr int kRingIdxBits = 23;
+constexpr unsigned kRingIdxMask = (1u << kRingIdxBits) - 1u;
+static_assert(4 * kMaxBoxPx <= (size_t)kRingIdxMask + 1, "box positions must fit the key's low bits");
+static_assert(kMaxBoxPx < (1u << 20), "dx^2 + dy^2 must fit the key's high 41 bits");
+
+// The square ring at Chebyshev distance r >= 1, clipped to the box
+// |dx| < bw, |dy| < bh, as four runs: top (dy = -r, dx rising from -r), right
+// (dx = r, dy rising from -r), bottom (dy = r, dx falling from r) and left
+// (dx = -r, dy falling from r); each corner belongs to one run.
+struct RingRuns {
+  int lo[4], len[4];
+};
+
+__device__ __forceinline__ RingRuns ring_runs(int r, int bw, int bh) {
+  RingRuns R;
+  const bool rows = r < bh, cols = r < bw;
+  // top: dx in [max(-r, 1-bw), min(r-1, bw-1)]
+  R.lo[0] = max(-r, 1 - bw);
+  R.len[0] = rows ? max(0, min(r - 1, bw - 1) - R.lo[0] + 1) : 0;
+  // right: dy in [max(-r, 1-bh), min(r-1, bh-1)]
+  R.lo[1] = max(-r, 1 - bh);
+  R.len[1] = cols ? max(0, min(r - 1, bh - 1) - R.lo[1] + 1) : 0;
+  // bottom: dx falling from min(r, bw-1) to max(1-r, 1-bw)
+  R.lo[2] = min(r, bw - 1);
+  R.len[2] = rows ? max(0, R.lo[2] - max(1 - r, 1 - bw) + 1) : 0;
+  // left: dy falling from min(r, bh-1) to max(1-r, 1-bh)
+  R.lo[3] = min(r, bh - 1);
+  R.len[3] = cols ? max(0, R.lo[3] - max(1 - r, 1 - bh) + 1) : 0;
+  return R;
+}
+
+__device__ __forceinline__ int ring_count(int r, int bw, int bh) {
+  const RingRuns R = ring_runs(r, bw, bh);
+  return R.len[0] + R.len[1] + R.len[2] + R.len[3];
+}
+
+// Point k (0 <= k < ring_count) of the clipped ring r.
+__device__ __forceinline__ void ring_point(int r, int k, int bw, int bh, int& dx, int& dy) {
+  const RingRuns R = ring_runs(r, bw, bh);
+  if (k < R.len[0]) { dx = R.lo[0] + k; dy = -r; return; }
+  k -= R.len[0];
+  if (k < R.len[1]) { dx = r; dy = R.lo[1] + k; return; }
+  k -= R.len[1];
+  if (k < R.len[2]) { dx = R.lo[2] - k; dy = r; return; }
+  k -= R.len[2];
+  dx = -r;
+  dy = R.lo[3] - k;
 }
 
 // prepare_neighbors by rings: every offset of the box, ring by ring, goes
 // through the same sorted insertion as build_patch_sparse (key: dx^2 + dy^2,
-// then descending box position -- the sorted offset list's order); the scan
-// stops once the patch is full and a ring lies wholly beyond its last entry.
+// then descending box position -- the sorted offset list's order).  Only the
+// parts of a ring inside the box are visited, and a warp pass covers the
+// points of up to 32 consecutive rings (a thin box has two points per ring),
+// so the work per target is O(box pixels / 32) warp passes at worst.  The
+// scan stops once the patch is full and the next ring lies wholly beyond its
+// last entry.
 __device__ int build_patch_rings(const Problem& pb, int px, int py, Patch& P, unsigned long long* best, int lane) {
   if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
   const int lim = pb.patchLimit - 1;
@@ -1550,20 +1600,44 @@ __device__ int build_patch_rings(const Problem& pb, int px, int py, Patch& P, un
   const int rmax = max(bw, bh) - 1;
   int cnt = 0;
   unsigned long long thr = ~0ull;
-  for (int r = 1; r <= rmax; r++) {
-    if (cnt == lim && (unsigned long long)r * r > (thr >> 32)) break;
-    for (int base = 0; base < 8 * r; base += 32) {
-      const int k = base + lane;
+  bool done = false;
+  for (int r0 = 1; r0 <= rmax && !done; r0 += 32) {
+    // rings r0 .. r0 + 31: lane j counts ring r0 + j, an inclusive scan gives
+    // where each ring's points start in this group
+    const int myR = r0 + lane;
+    const int myC = myR <= rmax ? ring_count(myR, bw, bh) : 0;
+    int incl = myC;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    for (int base = 0; base < total; base += 32) {
+      // the ring of this pass's first point: every later point is as far
+      const int g0 = base;
+      int j0 = 0;
+      for (int s = 16; s >= 1; s >>= 1)
+        if (__shfl_sync(kFull, incl, j0 + s - 1) <= g0) j0 += s;
+      const int rFirst = r0 + j0;
+      if (cnt == lim && (unsigned long long)rFirst * rFirst > (thr >> kRingIdxBits)) {
+        done = true;
+        break;
+      }
+      const int g = base + lane;
+      int j = 0;
+      for (int s = 16; s >= 1; s >>= 1)
+        if (__shfl_sync(kFull, incl, j + s - 1) <= g) j += s;
+      j = min(j, 31);
+      const int inclJ = __shfl_sync(kFull, incl, j), cJ = __shfl_sync(kFull, myC, j);
       unsigned long long key = ~0ull;
-      if (k < 8 * r) {
+      if (g < total) {
         int dx, dy;
-        ring_point(r, k, dx, dy);
-        if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
-          int qx = px + dx, qy = py + dy;
-          if (wrap_or_clip(pb, qx, qy) && pb.has[qy * pb.tw + qx]) {
-            const unsigned idx = (unsigned)(dy + bh - 1) * W2 + (unsigned)(dx + bw - 1);
-            key = ((unsigned long long)(dx * dx + dy * dy) << 32) | (0xFFFFFFFFu - idx);
-          }
+        ring_point(r0 + j, g - (inclJ - cJ), bw, bh, dx, dy);
+        int qx = px + dx, qy = py + dy;
+        if (wrap_or_clip(pb, qx, qy) && pb.has[(size_t)qy * pb.tw + qx]) {
+          const unsigned idx = (unsigned)(dy + bh - 1) * W2 + (unsigned)(dx + bw - 1);
+          const unsigned long long d2 = (unsigned long long)((long long)dx * dx + (long long)dy * dy);
+          key = (d2 << kRingIdxBits) | (unsigned long long)(kRingIdxMask - idx);
         }
       }
       unsigned m = __ballot_sync(kFull, key < thr);
@@ -1587,7 +1661,7 @@ __device__ int build_patch_rings(const Problem& pb, int px, int py, Patch& P, un
     }
   }
   for (int i = lane; i < cnt; i += 32) {
-    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
+    const unsigned idx = kRingIdxMask - (unsigned)(best[i] & kRingIdxMask);
     const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
     int qx = px + dx, qy = py + dy;
     wrap_or_clip(pb, qx, qy);
@@ -1662,8 +1736,11 @@ extern "C" __attribute__((visibility("default"))) int resynthFrozenBestFitNoAllo
       !dPatchCount || (n && (!dTargets || !dCands)))
     return rs_fail(RESYNTH_ERROR_ARGUMENT, "resynthFrozenBestFitNoAlloc: NULL argument");
   if (p->patchSize > (unsigned)kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
+  // Every byte the packing kernel reads (colours at 1 .. colorEndBip - 1, map
+  // channels at map_start_bip ..) must lie inside the caller's pixel.
   if (f->img_match_bpp < 1 || f->img_match_bpp > 3 || f->map_match_bpp > 3 || f->total_bpp > 8 ||
-      f->colorEndBip != 1 + f->img_match_bpp || !tw || !th || !cw || !ch)
+      f->colorEndBip != 1 + f->img_match_bpp || f->colorEndBip > f->total_bpp ||
+      (f->map_match_bpp && f->map_start_bip + f->map_match_bpp > f->total_bpp) || !tw || !th || !cw || !ch)
     return rs_fail(RESYNTH_ERROR_UNSUPPORTED, "resynthFrozenBestFitNoAlloc: pixel layout not supported");
   const bool maps = f->map_match_bpp > 0;
   const size_t tWords = (size_t)tw * th, cWords = (((size_t)cw * ch) + 3) & ~(size_t)3;

@@ -116,3 +116,42 @@ def test_reference_testsynth_links_unchanged(lib, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0
     assert "Test Gray w/o alpha" in r.stdout
+
+
+def test_layouts_reaching_past_the_pixel_are_rejected(lib):
+    """A TFormatIndices whose colour, map or alpha bytes lie past total_bpp is
+    refused with RESYNTH_ERROR_UNSUPPORTED before any device work (the
+    kernels would otherwise read past the end of the caller's buffers).  The
+    pointers are never dereferenced: the call must answer from the layout
+    alone."""
+    P = C.POINTER
+    lib.resynthFrozenBestFitNoAlloc.argtypes = [P(R.ImageSynthParameters), P(R.FormatIndices)] + [
+        C.c_void_p, C.c_uint, C.c_uint, C.c_void_p, C.c_uint, C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint,
+        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    p = R.params()
+    bad = []
+    f = R.format_indices(3, 1, 0, 0, 1)
+    f.total_bpp = 4                        # the map byte would be byte 4 of a 4-byte pixel
+    bad.append(f)
+    f = R.format_indices(3, 0, 0, 0, 0)
+    f.total_bpp = 3                        # colours end at byte 4
+    bad.append(f)
+    f = R.format_indices(2, 2, 0, 0, 1)
+    f.map_start_bip = 4                    # map channels 4..5 of a 5-byte pixel
+    bad.append(f)
+    dummy = C.c_void_p(16)
+    buf = np.zeros(4096, np.uint8)            # host buffers, large enough for any of these layouts
+    hb = C.c_void_p(buf.ctypes.data)
+    for f in bad:
+        rc = lib.resynthFrozenBestFitNoAlloc(C.byref(p), C.byref(f), dummy, 8, 8, dummy, 8, 8, dummy, dummy, dummy,
+                                             1, dummy, dummy, dummy, dummy, dummy, None)
+        assert rc == 101 and "layout" in R.last_error()
+        rc = lib.resynthFrozenBestFit(C.byref(p), C.byref(f), hb, 8, 8, hb, 8, 8, hb, hb, hb, 0, hb, hb, hb, hb, hb)
+        assert rc == 101
+    # alpha byte outside the pixel, through engine() on host maps
+    f = R.format_indices(3, 0, 1, 1, 0)
+    f.alpha_bip = 9
+    t = np.zeros((4, 4, f.total_bpp), np.uint8)
+    t[1:3, 1:3, 0] = 255
+    r = R.engine(t, t.copy(), f, R.params())
+    assert r.rc == 101

@@ -6,7 +6,8 @@ loop that cannot take cudaMalloc's implicit synchronisation).  The test owns
 every device buffer, calls the entry point through the C ABI twice in a row
 with different problems -- so the second call runs over the working array the
 first one left behind -- and requires results identical to the allocating
-entry point resynthFrozenBestFit (integer metric: exact equality)."""
+entry point resynthFrozenBestFit and to the CPU oracle's restatement of the
+reference computeBestFit (integer metric: exact equality)."""
 import ctypes as C
 
 import numpy as np
@@ -17,18 +18,17 @@ import resynthesizer_gb300 as R
 pytestmark = pytest.mark.gpu
 
 
-def _problem(seed, fmt, tw, th, cw, ch, tile):
+def _problem(seed, fmt, tw, th, cw, ch, tile, has_density=0.3, n=300):
     rng = np.random.default_rng(seed)
     bpp = 1 + fmt[0] + (1 if fmt[2] or fmt[3] else 0) + (fmt[1] if fmt[4] else 0)
     target = rng.integers(0, 256, (th, tw, bpp), dtype=np.uint8)
     corpus = rng.integers(0, 256, (ch, cw, bpp), dtype=np.uint8)
     corpus[..., 0] = np.where(rng.random((ch, cw)) < 0.9, 255, 0)
-    has = (rng.random((th, tw)) < 0.3).astype(np.uint8)
+    has = (rng.random((th, tw)) < has_density).astype(np.uint8)
     src = np.full((th, tw, 2), -1, np.int32)
     m = rng.random((th, tw)) < 0.6
     src[m, 0] = rng.integers(0, cw, m.sum())
     src[m, 1] = rng.integers(0, ch, m.sum())
-    n = 300
     targets = np.stack([rng.integers(0, tw, n), rng.integers(0, th, n)], 1).astype(np.int32)
     start = np.concatenate([[0], np.cumsum(rng.integers(0, 120, n))]).astype(np.uint32)
     cands = np.stack([rng.integers(-2, cw + 2, start[-1]), rng.integers(-2, ch + 2, start[-1])], 1).astype(np.int32)
@@ -75,16 +75,44 @@ def lib():
     return L
 
 
-def test_no_alloc_matches_allocating_entry_point_twice(lib):
+def _oracle(oracle, params, fmt, *arrays):
+    from oracle import Format, Params
+    op = Params(params.isMakeSeamlesslyTileableHorizontally, params.isMakeSeamlesslyTileableVertically,
+                params.matchContextType, params.mapWeight, params.sensitivityToOutliers, params.patchSize,
+                params.maxProbeCount)
+    of = Format(*(getattr(fmt, f) for f, _ in Format._fields_))
+    return oracle.frozen(op, of, *arrays)
+
+
+def _check(lib, oracle, prob):
+    got = _no_alloc(lib, *prob)
+    want = R.frozen_best_fit(*prob)
+    ref = _oracle(oracle, *prob)
+    for g, w, o in zip(got, want, ref):
+        assert np.array_equal(g, w)
+        assert np.array_equal(g, o)
+
+
+def test_no_alloc_matches_allocating_entry_point_twice(lib, oracle):
     problems = [
         _problem(101, (3, 0, 0, 0, 0), 90, 70, 60, 50, 0),      # RGB, no maps
         _problem(202, (3, 1, 0, 0, 1), 64, 80, 100, 40, 1),     # RGB + one map channel, tiled
     ]
     for prob in problems:                                      # two calls in a row
-        got = _no_alloc(lib, *prob)
-        want = R.frozen_best_fit(*prob)
-        for g, w in zip(got, want):
-            assert np.array_equal(g, w)
+        _check(lib, oracle, prob)
+
+
+def test_no_alloc_thin_boxes_and_sparse_values(lib, oracle):
+    # Thin and wide boxes with about 1 % of the pixels valued: patches are
+    # gathered from far along the box; odd pixel counts leave the working
+    # array's sections unaligned.
+    problems = [
+        _problem(303, (3, 0, 0, 0, 0), 3001, 3, 2001, 4, 0, has_density=0.01, n=200),
+        _problem(404, (1, 0, 0, 0, 0), 2, 3999, 3, 1501, 0, has_density=0.01, n=200),
+        _problem(505, (3, 1, 0, 0, 1), 4001, 2, 2999, 1, 1, has_density=0.02, n=150),
+    ]
+    for prob in problems:
+        _check(lib, oracle, prob)
 
 
 def test_no_alloc_rejects_oversized_images(lib):
