@@ -162,6 +162,8 @@ typedef struct {
   int graphs;                 /* wavefront: launch each pass as one captured CUDA graph */
   int separateRequests;       /* imageSynthBatch: one stream per request instead of the many-request launches */
   unsigned int bandGrowthLarge; /* wavefront: growth in percent of pass-0 bands of at least 1/64 of the pass (0 = default) */
+  int batchLaunches;          /* wavefront: one kernel launch per batch instead of one persistent (cooperative)
+                                 launch per pass with grid barriers between batches; the output is the same */
 } TResynthOptions;
 
 typedef struct {
@@ -317,6 +319,24 @@ int resynthTcGemm(const float *A, const float *B, int M, int N, int K, float *D)
  * up after a fixed number of polls.  Returns RESYNTH_ERROR_DEVICE ("a
  * tensor-core wait ran out") with the CUDA context still usable. */
 int resynthTcWaitTimeout(void);
+
+/* No counterpart in the reference.  Measures, on the current device, a peak
+ * of one of the two on-chip resources the synthesis kernels are bound by:
+ * which = 0: shared-memory load bandwidth (conflict-free 16-byte loads), in
+ * GB/s over the whole GPU; which = 1: 32-bit integer ALU throughput (chains
+ * of add and xor), in G ops/s.  Three warm-up launches, then the best of
+ * five timed with CUDA events; *ms (may be NULL) receives that launch's time. */
+int resynthMicrobench(int which, double *value, double *ms);
+
+/* No counterpart in the reference.  Test entry of the grid barrier the
+ * persistent wavefront kernel places between batches: a cooperative launch
+ * (two CTAs per SM) in which every CTA meets `rounds` barriers, except CTA
+ * absentCta (pass -1 for none), which leaves at once.  A barrier wait longer
+ * than timeoutNs nanoseconds gives up.  *passed receives the barriers passed
+ * summed over CTAs, *error the kernel's error bits (4 = a barrier wait ran
+ * out).  Returns 0 when the launch completed, with the CUDA context usable. */
+int resynthGridBarrierProbe(int rounds, int absentCta, long long timeoutNs, unsigned int *passed,
+                            unsigned int *error);
 
 /* No counterpart in the reference.  The proposal network reads an 11 x 11
  * context around a target pixel and emits 16 source offsets; in wavefront

@@ -60,7 +60,8 @@ class Options(C.Structure):
                 ("warpsPerBlock", C.c_uint), ("recordState", C.c_int), ("profile", C.c_int),
                 ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint),
                 ("net", C.c_void_p), ("proposals", C.c_uint), ("dumpPairs", C.c_void_p), ("dumpStride", C.c_uint),
-                ("graphs", C.c_int), ("separateRequests", C.c_int), ("bandGrowthLarge", C.c_uint)]
+                ("graphs", C.c_int), ("separateRequests", C.c_int), ("bandGrowthLarge", C.c_uint),
+                ("batchLaunches", C.c_int)]
 
 
 class TrainOptions(C.Structure):
@@ -183,7 +184,7 @@ def format_indices(colors, mapColors=0, alphaTarget=0, alphaSource=0, isMap=0) -
 
 def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, recordState=0,
             profile=0, phaseSide=0, bandGrowth=0, minPasses=0, net=None, proposals=0, dump=None,
-            dumpStride=0, graphs=0, separateRequests=0, bandGrowthLarge=0) -> Options:
+            dumpStride=0, graphs=0, separateRequests=0, bandGrowthLarge=0, batchLaunches=0) -> Options:
     o = Options()
     lib().resynthDefaultOptions(C.byref(o))
     if mode is not None:
@@ -197,6 +198,7 @@ def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, r
     o.dumpStride = dumpStride
     o.graphs = graphs
     o.separateRequests = separateRequests
+    o.batchLaunches = batchLaunches
     o.bandGrowthLarge = bandGrowthLarge
     return o
 
@@ -385,6 +387,33 @@ def image_synth_batch(items, opts: Options | None = None, concurrency: int = 8):
     st = Stats()
     rc = lib().imageSynthBatch(reqs, len(items), concurrency, C.byref(opts) if opts else None, C.byref(st))
     return rc, [k[0] for k in keep], [reqs[i].result for i in range(len(items))], st.as_dict()
+
+
+def grid_barrier_probe(rounds: int, absent_cta: int = -1, timeout_ns: int = 1_000_000_000):
+    """resynthGridBarrierProbe: (barriers passed summed over CTAs, error bits)."""
+    L = lib()
+    L.resynthGridBarrierProbe.argtypes = [C.c_int, C.c_int, C.c_longlong, C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
+    passed, err = C.c_uint(0), C.c_uint(0)
+    rc = L.resynthGridBarrierProbe(rounds, absent_cta, timeout_ns, C.byref(passed), C.byref(err))
+    if rc:
+        raise RuntimeError(f"resynthGridBarrierProbe rc={rc}: {last_error()}")
+    return passed.value, err.value
+
+
+def microbench(which: int):
+    """resynthMicrobench: (peak, ms): which 0 = shared-memory load GB/s, 1 = INT32 ALU G ops/s."""
+    L = lib()
+    L.resynthMicrobench.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    v, ms = C.c_double(0), C.c_double(0)
+    rc = L.resynthMicrobench(which, C.byref(v), C.byref(ms))
+    if rc:
+        raise RuntimeError(f"resynthMicrobench rc={rc}: {last_error()}")
+    return v.value, ms.value
+
+
+def sm_count() -> int:
+    import torch
+    return torch.cuda.get_device_properties(0).multi_processor_count
 
 
 def tc_gemm(a: np.ndarray, b: np.ndarray) -> np.ndarray:

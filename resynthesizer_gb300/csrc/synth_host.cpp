@@ -630,6 +630,11 @@ DeviceProblem make_problem(Arena& ar, cudaStream_t s, const TImageSynthParameter
 // and keep doubling.
 constexpr unsigned kDefaultGrowthLarge = 200;
 
+// A grid-barrier wait of the persistent wavefront kernel longer than this
+// gives up: far beyond the longest batch (milliseconds), short enough that a
+// CTA that never arrives ends the call with an error instead of holding the GPU.
+constexpr long long kBarrierTimeoutNs = 10LL * 1000 * 1000 * 1000;
+
 // Passes the wavefront runs at least.  Texture synthesis from nothing (no
 // context, no map channels) ends its second pass with a patch energy about
 // 1.5 % above the reference's threaded engine (the targets of a batch do not
@@ -882,6 +887,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     wa.sparseLimit2 = 4LL * dp.pb.patchLimit * (long long)ntargets;
     const bool sparseOk = noContext && !dp.pb.tileH && !dp.pb.tileV;
     wa.stageSrc = ar.alloc<int2>(ntargets);
+    rs::GridBar* gbar = ar.alloc<rs::GridBar>(1);
     int2* dPass = ar.alloc<int2>(ntargets);
     int* dBandEnds = ar.alloc<int>(kMaxBands);
     int* dBandPhased = ar.alloc<int>(kMaxBands);
@@ -987,7 +993,14 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       if (tuning)
         for (auto& e : tev) CK(cudaEventCreate(&e));
       int maxCtas = 0, maxCommit = 0;
-      for (int b = 0; b < nbatches; b++) {
+      // Persistent pass: the batches run in one cooperative launch with a grid
+      // barrier between them (a tuning pass first times its first three
+      // batches as single launches).  The proposal network runs between the
+      // bands, and graph capture records per-batch launches, so those passes
+      // keep one launch per batch.
+      const bool persistent = !opt.batchLaunches && !net && !graphPass && rs_persistent_supported();
+      const int singleEnd = persistent ? (tuning ? std::min(3, nbatches) : 0) : nbatches;
+      for (int b = 0; b < singleEnd; b++) {
         if (!phased[b / (k * k)] && b % (k * k)) continue;   // empty by construction
         if (b % (k * k) == 0) {
           // Grid cap from the band's expected batch size (its targets spread
@@ -1021,6 +1034,18 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
           launches++;
         }
         if (tuning && b == 2) CK(cudaEventRecord(tev[3], s));
+      }
+      // the rest of the pass, after the single launches it depends on
+      if (persistent && singleEnd < nbatches) {
+        wa.batch = singleEnd;
+        wa.batchEnd = nbatches;
+        wa.gbar = gbar;
+        wa.barTimeoutNs = kBarrierTimeoutNs;
+        CK(cudaMemsetAsync(gbar, 0, sizeof(rs::GridBar), s));
+        if (opt.profile) prof.begin(s);
+        CK(rs_launch_wave_persistent(wa, warps, s));
+        if (opt.profile) prof.end(s);
+        launches += 2;
       }
       cudaGraphExec_t passExec = nullptr;
       if (graphPass) {

@@ -50,6 +50,19 @@ struct Problem {
 constexpr int kCellShift = 3;
 constexpr int kCell = 1 << kCellShift;
 
+// Grid-wide barrier of the persistent wavefront kernel (cooperative launch):
+// zeroed by the host before every launch.
+struct GridBar {
+  unsigned int count;            // CTAs arrived in the current generation
+  unsigned int gen;              // generation, advanced by the last CTA to arrive
+  unsigned int stop;             // written by that CTA: nonzero = every CTA leaves
+  unsigned int pad;
+};
+
+// Counters::error bits.
+constexpr unsigned kErrStage = 1u;     // a bulk copy into shared memory did not complete
+constexpr unsigned kErrBarrier = 4u;   // a grid-barrier wait ran out (a CTA never arrived)
+
 // Device counters accumulated by the synthesis kernels.
 struct Counters {
   unsigned long long evals;
@@ -94,6 +107,12 @@ struct WaveArgs {
   int propBatch0;                // the band's first batch: props index = t - batchStart[propBatch0]
   int probeShare;                // random probes keyed by (batch, slot / 16) instead of the pixel
   int nbatches;                  // many-request steps: batches of this pass (0 = inactive)
+  // Persistent kernel (one cooperative launch runs batches batch .. batchEnd - 1
+  // with a grid barrier after each, and a commit phase between barriers when
+  // results are staged):
+  int batchEnd;
+  GridBar* gbar;
+  long long barTimeoutNs;        // a barrier wait longer than this gives up (kErrBarrier)
 };
 
 // Frozen-state scoring and energy.
@@ -122,6 +141,10 @@ cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc,
 cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream_t s);
 cudaError_t rs_launch_wave(const rs::WaveArgs& a, int warpsPerBlock, int maxCtas, cudaStream_t s);
 cudaError_t rs_launch_commit(const rs::WaveArgs& a, int maxCtas, cudaStream_t s);
+// Batches a.batch .. a.batchEnd - 1 of one problem in one cooperative launch.
+cudaError_t rs_launch_wave_persistent(const rs::WaveArgs& a, int warpsPerBlock, cudaStream_t s);
+// Whether this device can run the persistent kernel (cooperative launches).
+int rs_persistent_supported();
 int rs_wave_corpus_staged(const rs::Problem& pb, int warps);
 cudaError_t rs_launch_wave_multi(const rs::WaveArgs* jobs, int nreq, const int* prefix, int step, int visCur, int nc,
                                  int map, int maxCtas, const volatile int* abortFlag, cudaStream_t s);

@@ -23,7 +23,10 @@
 #include <map>
 #include <mutex>
 
+#include "../../include/resynthesizer.h"
 #include "synth_internal.h"
+
+extern "C" int rs_fail(int code, const char* msg);
 
 namespace rs {
 namespace {
@@ -1083,6 +1086,181 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
   }
 }
 
+// ------------------------------------------------ persistent wavefront pass
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Barrier across every CTA of a cooperative launch.  Thread 0 of each CTA
+// publishes the CTA's writes (fence), arrives, and waits for the generation
+// to advance; the last CTA to arrive decides for everyone whether the run
+// stops here (the host's abort flag, or an error any CTA reported before
+// arriving) and releases the others.  A wait gives up after timeoutNs of
+// global time: the CTA records kErrBarrier and leaves, so a CTA that never
+// arrives makes every other CTA leave at its next barrier instead of
+// spinning forever.  Returns true when the CTA must leave.
+__device__ bool grid_barrier(GridBar* gb, const volatile int* abortFlag, unsigned* err, long long timeoutNs) {
+  __shared__ unsigned s_stop;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned gen = ld_acquire_gpu(&gb->gen);
+    __threadfence();
+    const unsigned arrived = atomicAdd(&gb->count, 1u);
+    unsigned stop = 0;
+    if (arrived == gridDim.x - 1) {
+      __threadfence();
+      stop = (*abortFlag != 0 || *(volatile unsigned*)err != 0u) ? 1u : 0u;
+      atomicExch(&gb->count, 0u);
+      *(volatile unsigned*)&gb->stop = stop;
+      st_release_gpu(&gb->gen, gen + 1u);
+    } else {
+      const unsigned long long t0 = global_ns();
+      bool late = false;
+      while (ld_acquire_gpu(&gb->gen) == gen) {
+        if ((long long)(global_ns() - t0) > timeoutNs) {
+          late = true;
+          break;
+        }
+        __nanosleep(64);
+      }
+      if (late) {
+        atomicOr(err, kErrBarrier);
+        stop = 1u;
+      } else {
+        stop = *(volatile unsigned*)&gb->stop;
+      }
+    }
+    s_stop = stop;
+  }
+  __syncthreads();
+  return s_stop != 0u;
+}
+
+// Applies the staged results of batch `batch` (grid-stride over its slots);
+// returns how many of this thread's slots changed source.
+__device__ __forceinline__ unsigned commit_batch(const WaveArgs& a, int batch) {
+  const Problem& pb = a.pb;
+  const int b0 = a.batchStart[batch];
+  const int nslots = a.batchStart[batch + 1] - b0;
+  unsigned better = 0;
+  for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < nslots; slot += gridDim.x * blockDim.x) {
+    const int2 pos = a.targets[b0 + slot];
+    const int pi = pos.y * pb.tw + pos.x;
+    const int2 s = a.stageSrc[slot];
+    if (s.x != -2) {
+      const uint32_t c = pb.cpx[s.y * pb.cw + s.x];
+      pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (c & 0xFFFFFF00u);
+      pb.src[pi] = s;
+      better++;
+    }
+    if (!pb.vis) pb.has[pi] = 1;
+  }
+  return better;
+}
+
+// Batches a.batch .. a.batchEnd - 1 of one pass in one launch: the corpus is
+// staged into shared memory once, each batch runs as in k_wave (a team of
+// warps per target, sized to the batch), then every CTA meets at a grid
+// barrier before the next batch reads the state; staged passes apply their
+// results between two barriers.  The outputs are those of one k_wave (+
+// k_commit) launch per batch: the same targets, in the same batches, see the
+// same state.  Needs a cooperative launch (every CTA resident).
+template <int NC, bool MAP, bool SMEMC>
+__global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* ct = reinterpret_cast<uint32_t*>(smem);
+  uint32_t* mt = ct + 256;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(mt + 256);
+  unsigned char* p = smem + WaveSmem::kHead;
+  const Problem& pb = a.pb;
+  const int padH = pb.ch + 2 * kPad;
+  auto cv = padded_view<MAP>(pb);
+  const unsigned cwords = ((unsigned)(pb.padW * padH) + 3u) & ~3u;
+  bool ok = true;
+  if (SMEMC) {
+    if constexpr (MAP) {
+      uint2* scpm = reinterpret_cast<uint2*>(p);
+      p += cwords * 8;
+      ok = stage_words(reinterpret_cast<uint32_t*>(scpm), reinterpret_cast<const uint32_t*>(pb.cpmPad), cwords * 2,
+                       bar);
+      cv.pm = scpm;
+    } else {
+      uint32_t* scpx = reinterpret_cast<uint32_t*>(p);
+      p += cwords * 4;
+      ok = stage_words(scpx, pb.cpxPad, cwords, bar);
+      cv.px = scpx;
+    }
+    // A CTA whose copy failed does no work but still meets every barrier; the
+    // barrier's leader sees the error and stops the run for all.
+    if (!ok && threadIdx.x == 0) atomicOr(&a.ctr->error, kErrStage);
+  }
+  load_half_tables(pb, ct, mt);
+  __shared__ unsigned long long s_key[16];
+  __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16];
+  __shared__ unsigned s_better;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  if (threadIdx.x == 0) s_better = 0;
+  __syncthreads();
+  unsigned terms = 0, evals = 0, committed = 0;
+  for (int b = a.batch; b < a.batchEnd; b++) {
+    const int b0 = a.batchStart[b];
+    const int nslots = a.batchStart[b + 1] - b0;
+    // An empty batch changes nothing: every CTA reads the same boundaries, so
+    // all of them skip its barriers together.
+    if (nslots == 0) continue;
+    if (ok) {
+      const int G = team_size(nslots);
+      const int teamsPerBlock = wpb / G;
+      const int team = warp / G;
+      const WaveTeam T{G, team, warp % G, team * G, lane, warp, p, s_key, s_n, s_np, s_fast, s_gather};
+      const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
+      const int visCur = a.pass == 0 ? b : 0x7ffffffe;
+      for (int slot = blockIdx.x * teamsPerBlock + team; slot < nslots; slot += gridDim.x * teamsPerBlock) {
+        const unsigned better = wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
+        if (better) atomicAdd(&s_better, 1u);
+      }
+    }
+    if (!a.inPlace) {
+      if (grid_barrier(a.gbar, a.abortFlag, &a.ctr->error, a.barTimeoutNs)) break;
+      committed += commit_batch(a, b);
+    }
+    if (grid_barrier(a.gbar, a.abortFlag, &a.ctr->error, a.barTimeoutNs)) break;
+  }
+  for (int o = 16; o > 0; o >>= 1) committed += __shfl_xor_sync(kFull, committed, o);
+  if (lane == 0 && committed) atomicAdd(&s_better, committed);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_better) atomicAdd(&a.ctr->betters, s_better);
+  const unsigned long long tv = warp_sum_u64(terms), ev = warp_sum_u64(evals);
+  if (lane == 0) {
+    atomicAdd(&a.ctr->terms, tv);
+    atomicAdd(&a.ctr->evals, ev);
+  }
+}
+
+// Test kernel of the grid barrier: every CTA but CTA `absent` meets `rounds`
+// barriers; CTA `absent` (when in range) leaves at once, so the others' waits
+// must run out.
+__global__ void k_barrier_probe(GridBar* gb, const volatile int* abortFlag, unsigned* err, int rounds, int absent,
+                                long long timeoutNs, unsigned* passed) {
+  if ((int)blockIdx.x == absent) return;
+  for (int r = 0; r < rounds; r++) {
+    if (grid_barrier(gb, abortFlag, err, timeoutNs)) return;
+    if (threadIdx.x == 0) atomicAdd(passed, 1u);
+  }
+}
+
 // The request of global slot gs: prefix[r] <= gs < prefix[r + 1].
 __device__ __forceinline__ int multi_request(const int* prefix, int nreq, int gs) {
   int lo = 0, hi = nreq - 1;
@@ -1441,6 +1619,101 @@ extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, int maxCtas,
 }
 
 namespace {
+template <int NC, bool MAP, bool SMEMC>
+cudaError_t launch_wave_persistent_t(const WaveArgs& a, int warps, size_t smem, cudaStream_t s) {
+  auto kern = k_wave_persistent<NC, MAP, SMEMC>;
+  static std::mutex mu;
+  static size_t configured = 0;
+  static std::map<std::pair<size_t, int>, int> perSmCache;
+  static int carvePct = 0;
+  int perSm = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (smem > configured) {
+      const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = smem;
+    }
+    auto it = perSmCache.find({smem, warps});
+    if (it == perSmCache.end()) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
+      if (!SMEMC && perSm > 0) prefer_l1(kern, warps * 32, smem, perSm, carvePct);
+      // the occupancy after the carveout hint is what a cooperative launch is checked against
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
+      perSmCache[{smem, warps}] = perSm;
+    } else {
+      perSm = it->second;
+    }
+  }
+  if (perSm < 1) return cudaErrorInvalidConfiguration;
+  // One CTA per resident slot: every CTA is on the GPU at once, which the grid
+  // barrier needs (the cooperative launch refuses a grid that could not be).
+  WaveArgs args = a;
+  void* params[] = {&args};
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(sm_count() * perSm), dim3(warps * 32), params, smem, s);
+}
+}  // namespace
+
+extern "C" cudaError_t rs_launch_wave_persistent(const WaveArgs& a, int warps, cudaStream_t s) {
+  if (warps < 1) warps = 16;
+  if (warps > 16) warps = 16;
+  const size_t smemCorpus = wave_smem(a.pb, true, warps);
+  const bool smemc = smemCorpus <= 112 * 1024;   // two CTAs per SM
+  const size_t smem = smemc ? smemCorpus : wave_smem(a.pb, false, warps);
+  cudaError_t e = cudaSuccess;
+  if (smemc) {
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_persistent_t<NC, MAP, true>(a, warps, smem, s)));
+  } else {
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_persistent_t<NC, MAP, false>(a, warps, smem, s)));
+  }
+  return e;
+}
+
+extern "C" int rs_persistent_supported() {
+  static const int v = [] {
+    int dev = 0, c = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&c, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess) return 0;
+    return c;
+  }();
+  return v;
+}
+
+// No counterpart in the reference.  Test entry of the grid barrier of the
+// persistent kernel (declared in include/resynthesizer.h).
+extern "C" __attribute__((visibility("default"))) int resynthGridBarrierProbe(int rounds, int absentCta,
+                                                                               long long timeoutNs,
+                                                                               unsigned* passed, unsigned* error) {
+  if (!passed || !error || rounds < 0) return rs_fail(RESYNTH_ERROR_ARGUMENT, "resynthGridBarrierProbe: bad argument");
+  if (!rs_persistent_supported()) return rs_fail(RESYNTH_ERROR_DEVICE, "cooperative launches not supported");
+  struct Dev {
+    GridBar gb;
+    int abortFlag;
+    unsigned err, passed, pad;
+  };
+  Dev* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(Dev));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(Dev));
+  const int grid = sm_count() * 2;
+  if (e == cudaSuccess) {
+    GridBar* gb = &d->gb;
+    const volatile int* ab = &d->abortFlag;
+    unsigned* err = &d->err;
+    unsigned* pass = &d->passed;
+    void* params[] = {&gb, (void*)&ab, &err, &rounds, &absentCta, &timeoutNs, &pass};
+    e = cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(grid), dim3(256), params, 0, nullptr);
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  Dev h{};
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(Dev), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  if (e != cudaSuccess) return rs_fail(RESYNTH_ERROR_DEVICE, cudaGetErrorString(e));
+  *passed = h.passed;
+  *error = h.err;
+  return 0;
+}
+
+namespace {
 template <int NC, bool MAP>
 cudaError_t launch_wave_multi_t(const WaveArgs* jobs, int nreq, const int* prefix, int step, int visCur, int maxCtas,
                                 const volatile int* abortFlag, cudaStream_t s) {
@@ -1515,11 +1788,6 @@ extern "C" cudaError_t rs_launch_commit(const WaveArgs& a, int maxCtas, cudaStre
 // instead of walking a sorted offset list, so no list has to be stored.
 // ====================================================================
 
-#include <mutex>
-
-#include "../../include/resynthesizer.h"
-
-extern "C" int rs_fail(int code, const char* msg);
 extern "C" void rs_metric_tables(double sensitivity, double mapWeight, uint32_t* ct, uint32_t* mt);
 
 namespace rs {
