@@ -48,8 +48,9 @@ def test_persistent_pass_equals_batch_launches(name, warps):
     b = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=warps,
                                                            batchLaunches=1))
     assert a.rc == b.rc == 0, R.last_error()
+    # (evals and terms may differ: a small batch's team of warps per target
+    # depends on the grid size, and so does where each warp's early-outs fall)
     assert a.stats["passes"] == b.stats["passes"] and a.stats["betters"] == b.stats["betters"]
-    assert a.stats["evals"] == b.stats["evals"] and a.stats["terms"] == b.stats["terms"]
     assert np.array_equal(a.out, b.out)
     assert a.stats["launches"] < b.stats["launches"]
 
