@@ -1341,6 +1341,13 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
   rs::WaveArgs* dJobs = ar.alloc<rs::WaveArgs>(jobs.size());
   int* dPrefix = ar.alloc<int>(jobs.size() + 1);
   std::vector<rs::WaveArgs> hJobs;
+  // Persistent passes (one cooperative launch per pixel layout and pass), or
+  // one launch per step with options->batchLaunches.
+  const bool persistent = !opt.batchLaunches && rs_persistent_supported();
+  rs::GridBar* gbar = ar.alloc<rs::GridBar>(1);
+  CK(cudaMemsetAsync(gbar, 0, sizeof(rs::GridBar), s));
+  unsigned* barErr = reinterpret_cast<unsigned*>(st.hostInts + 8);   // pinned: read back with the counters
+  *barErr = 0;
   for (int pass = 0; pass < rs::kPasses; pass++) {
     std::vector<size_t> act;
     for (size_t i = 0; i < jobs.size(); i++)
@@ -1417,6 +1424,24 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       CK(cudaMemcpyAsync(dJobs, hJobs.data(), hJobs.size() * sizeof(rs::WaveArgs), cudaMemcpyHostToDevice, s));
       h2d += hJobs.size() * sizeof(rs::WaveArgs);
       const int n = (int)idx.size();
+      if (persistent) {
+        // The whole pass of this layout's requests in one cooperative launch
+        // per chunk of requests: every step's slot prefix first, then the
+        // steps with a work queue each and a grid barrier between them.
+        for (int c0 = 0; c0 < n; c0 += rs::kMultiPersistentMaxRequests) {
+          const int cn = std::min(n - c0, rs::kMultiPersistentMaxRequests);
+          int* dPrefixAll = ar.alloc<int>((size_t)steps * (cn + 1));
+          unsigned* dQueue = ar.alloc<unsigned>((size_t)steps);
+          CK(rs_launch_multi_prefix_all(dJobs + c0, cn, steps, dPrefixAll, s));
+          CK(cudaMemsetAsync(dQueue, 0, (size_t)steps * sizeof(unsigned), s));
+          // count, generation and stop word; the error word collects the whole call
+          CK(cudaMemsetAsync(gbar, 0, offsetof(rs::GridBar, error), s));
+          CK(rs_launch_wave_multi_persistent(dJobs + c0, cn, steps, dPrefixAll, dQueue, pass, staged ? 1 : 0, gbar,
+                                             st.abortDev, g.first.first, g.first.second, kBarrierTimeoutNs, s));
+          launches += 2;
+        }
+        continue;
+      }
       for (int b = 0; b < steps; b++) {
         // grid cap from the expected step size: each request's band spread
         // over its k * k phases, twice that for the spread
@@ -1440,10 +1465,12 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       }
     }
     CK(cudaMemcpyAsync(hostCtr.data(), ctrs, jobs.size() * sizeof(rs::Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(barErr, &gbar->error, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
     for (size_t i : act)
       CK(cudaMemcpyAsync(&visited[i], jobs[i].batchStart + jobs[i].wa.nbatches, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(epass, s));
     wait_stream(st, epass, nullptr);
+    if (*barErr) return fail(RESYNTH_ERROR_DEVICE, "many-request wavefront kernel reported error %u", *barErr);
     for (size_t i : act) {
       BatchJob& J = jobs[i];
       const rs::Counters& c = hostCtr[i];

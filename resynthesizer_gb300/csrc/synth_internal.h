@@ -56,8 +56,12 @@ struct GridBar {
   unsigned int count;            // CTAs arrived in the current generation
   unsigned int gen;              // generation, advanced by the last CTA to arrive
   unsigned int stop;             // written by that CTA: nonzero = every CTA leaves
-  unsigned int pad;
+  unsigned int error;            // error bits of a launch that has no Counters of its own (many requests)
 };
+
+// Most requests one persistent many-request launch takes (its slot prefix
+// sits in shared memory).
+constexpr int kMultiPersistentMaxRequests = 4096;
 
 // Counters::error bits.
 constexpr unsigned kErrStage = 1u;     // a bulk copy into shared memory did not complete
@@ -149,6 +153,14 @@ int rs_wave_corpus_staged(const rs::Problem& pb, int warps);
 cudaError_t rs_launch_wave_multi(const rs::WaveArgs* jobs, int nreq, const int* prefix, int step, int visCur, int nc,
                                  int map, int maxCtas, const volatile int* abortFlag, cudaStream_t s);
 cudaError_t rs_launch_multi_prefix(const rs::WaveArgs* jobs, int nreq, int step, int* prefix, cudaStream_t s);
+// Every step's slot prefix (steps x (nreq + 1) ints) for the persistent many-request pass.
+cudaError_t rs_launch_multi_prefix_all(const rs::WaveArgs* jobs, int nreq, int steps, int* prefix, cudaStream_t s);
+// Steps 0 .. steps - 1 of a pass of many requests of one pixel layout in one cooperative launch.
+cudaError_t rs_launch_wave_multi_persistent(const rs::WaveArgs* jobs, int nreq, int steps, const int* prefix,
+                                            unsigned* queue, int pass, int staged, rs::GridBar* gb,
+                                            const volatile int* abortFlag, int nc, int map, long long timeoutNs,
+                                            cudaStream_t s);
+
 cudaError_t rs_launch_commit_multi(const rs::WaveArgs* jobs, int nreq, const int* prefix, int step, int maxCtas,
                                    cudaStream_t s);
 cudaError_t rs_launch_frozen(const rs::ScoreArgs& a, cudaStream_t s);

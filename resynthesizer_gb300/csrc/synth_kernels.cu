@@ -1314,6 +1314,123 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi(const WaveArgs* jobs, int
   }
 }
 
+// A pass of many problems in one launch: steps 0 .. steps - 1, step b being
+// batch b of every request that has one.  prefix[b * (nreq + 1) + r] is the
+// first slot of request r in step b (prefix[... + nreq] = the step's total).
+// Work is handed out through a queue per step (queue[b], zeroed by the host):
+// a team takes the next slot as soon as it finishes one, so requests of
+// uneven cost share the GPU evenly.  A grid barrier closes each step (and,
+// when some request stages its results, a commit phase between two
+// barriers).  Results equal one k_wave_multi (+ k_commit_multi) launch per
+// step.  Needs a cooperative launch.
+template <int NC, bool MAP>
+__global__ void __launch_bounds__(512, 2) k_wave_multi_persistent(const WaveArgs* jobs, int nreq, int steps,
+                                                                  const int* prefix, unsigned* queue, int pass,
+                                                                  int staged, GridBar* gb,
+                                                                  const volatile int* abortFlag, unsigned* err,
+                                                                  long long timeoutNs) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int wpb = blockDim.x >> 5;
+  int* sPrefix = reinterpret_cast<int*>(smem + WaveSmem::kHead + wpb * WaveSmem::kPerWarp);
+  __shared__ unsigned long long s_key[16];
+  __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16], s_item[16];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = 0; b < steps; b++) {
+    const int* pre = prefix + (size_t)b * (nreq + 1);
+    const int total = pre[nreq];
+    if (total == 0) continue;   // the same for every CTA: no barrier needed
+    for (int r = threadIdx.x; r <= nreq; r += blockDim.x) sPrefix[r] = pre[r];
+    __syncthreads();
+    const int G = team_size(total);
+    const int team = warp / G;
+    const WaveTeam T{G, team, warp % G, team * G, lane, warp, smem + WaveSmem::kHead, s_key, s_n, s_np, s_fast,
+                     s_gather};
+    const int visCur = pass == 0 ? b : 0x7ffffffe;
+    if (T.tw == 0 && lane == 0) s_item[team] = (int)atomicAdd(&queue[b], 1u);
+    T.sync();
+    int gs = s_item[team];
+    while (gs < total) {
+      int nxt = 0;
+      if (T.tw == 0 && lane == 0) nxt = (int)atomicAdd(&queue[b], 1u);   // in flight while this slot runs
+      const int r = multi_request(sPrefix, nreq, gs);
+      const WaveArgs& a = jobs[r];
+      const Problem& pb = a.pb;
+      const auto cv = padded_view<MAP>(pb);
+      const int b0 = a.batchStart[b];
+      const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
+      unsigned terms = 0, evals = 0;
+      const unsigned better = wave_target<NC, MAP>(a, pb, cv, pb.ctab + 256, pb.mtab + 256, b, visCur, b0,
+                                                   gs - sPrefix[r], sparse, T, terms, evals);
+      if (better) atomicAdd(&a.ctr->betters, 1u);
+      const unsigned long long tv = warp_sum_u64(terms), ev = warp_sum_u64(evals);
+      if (lane == 0) {
+        atomicAdd(&a.ctr->terms, tv);
+        atomicAdd(&a.ctr->evals, ev);
+      }
+      if (T.tw == 0 && lane == 0) s_item[team] = nxt;
+      T.sync();
+      gs = s_item[team];
+    }
+    if (staged) {
+      if (grid_barrier(gb, abortFlag, err, timeoutNs)) return;
+      for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int r = multi_request(sPrefix, nreq, g);
+        const WaveArgs& a = jobs[r];
+        if (a.inPlace) continue;
+        const Problem& pb = a.pb;
+        const int slot = g - sPrefix[r];
+        const int2 pos = a.targets[a.batchStart[b] + slot];
+        const int pi = pos.y * pb.tw + pos.x;
+        const int2 s = a.stageSrc[slot];
+        if (s.x != -2) {
+          const uint32_t c = pb.cpx[s.y * pb.cw + s.x];
+          pb.tpx[pi] = (pb.tpx[pi] & 0xFFu) | (c & 0xFFFFFF00u);
+          pb.src[pi] = s;
+          atomicAdd(&a.ctr->betters, 1u);
+        }
+      }
+    }
+    if (grid_barrier(gb, abortFlag, err, timeoutNs)) return;
+  }
+}
+
+// Every step's exclusive slot prefix over the requests: one CTA per step.
+__global__ void __launch_bounds__(1024) k_multi_prefix_all(const WaveArgs* jobs, int nreq, int* prefix) {
+  __shared__ int warpSums[32];
+  __shared__ int carry;
+  const int step = blockIdx.x;
+  int* out = prefix + (size_t)step * (nreq + 1);
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < nreq; base += 1024) {
+    const int r = base + threadIdx.x;
+    int v = 0;
+    if (r < nreq && step < jobs[r].nbatches) v = jobs[r].batchStart[step + 1] - jobs[r].batchStart[step];
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = warpSums[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warpSums[lane] = w;
+    }
+    __syncthreads();
+    if (r < nreq) out[r] = carry + (warp ? warpSums[warp - 1] : 0) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warpSums[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[nreq] = carry;
+}
+
 // Slot counts of step `step` for every request (0 past its last batch or when
 // inactive) and their exclusive prefix; one CTA of 1024 threads.
 __global__ void __launch_bounds__(1024) k_multi_prefix(const WaveArgs* jobs, int nreq, int step, int* prefix) {
@@ -1739,6 +1856,62 @@ cudaError_t launch_wave_multi_t(const WaveArgs* jobs, int nreq, const int* prefi
   return cudaGetLastError();
 }
 }  // namespace
+
+namespace {
+template <int NC, bool MAP>
+cudaError_t launch_wave_multi_persistent_t(const WaveArgs* jobs, int nreq, int steps, const int* prefix,
+                                           unsigned* queue, int pass, int staged, GridBar* gb,
+                                           const volatile int* abortFlag, long long timeoutNs, cudaStream_t s) {
+  auto kern = k_wave_multi_persistent<NC, MAP>;
+  constexpr int warps = 16;
+  const size_t smem = WaveSmem::kHead + (size_t)warps * WaveSmem::kPerWarp + ((((size_t)nreq + 1) * 4 + 15) & ~(size_t)15);
+  static std::mutex mu;
+  static size_t configured = 0;
+  static std::map<size_t, int> perSmCache;
+  static int carvePct = 0;
+  int perSm = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (smem > configured) {
+      const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      configured = smem;
+    }
+    auto it = perSmCache.find(smem);
+    if (it == perSmCache.end()) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
+      if (perSm > 0) prefer_l1(kern, warps * 32, smem, perSm, carvePct);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, warps * 32, smem);
+      perSmCache[smem] = perSm;
+    } else {
+      perSm = it->second;
+    }
+  }
+  if (perSm < 1) return cudaErrorInvalidConfiguration;
+  unsigned* err = &gb->error;
+  void* params[] = {(void*)&jobs, &nreq, &steps, (void*)&prefix, &queue, &pass, &staged, &gb, (void*)&abortFlag,
+                    &err, &timeoutNs};
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(sm_count() * perSm), dim3(warps * 32), params, smem, s);
+}
+}  // namespace
+
+extern "C" cudaError_t rs_launch_wave_multi_persistent(const WaveArgs* jobs, int nreq, int steps, const int* prefix,
+                                                       unsigned* queue, int pass, int staged, GridBar* gb,
+                                                       const volatile int* abortFlag, int nc, int map,
+                                                       long long timeoutNs, cudaStream_t s) {
+  if (nreq < 1 || nreq > kMultiPersistentMaxRequests) return cudaErrorInvalidValue;
+  cudaError_t e = cudaSuccess;
+  RS_DISPATCH(nc, map != 0, (e = launch_wave_multi_persistent_t<NC, MAP>(jobs, nreq, steps, prefix, queue, pass,
+                                                                         staged, gb, abortFlag, timeoutNs, s)));
+  return e;
+}
+
+extern "C" cudaError_t rs_launch_multi_prefix_all(const WaveArgs* jobs, int nreq, int steps, int* prefix,
+                                                  cudaStream_t s) {
+  if (steps < 1) return cudaSuccess;
+  k_multi_prefix_all<<<steps, 1024, 0, s>>>(jobs, nreq, prefix);
+  return cudaGetLastError();
+}
 
 // Step `step` of many problems of one pixel layout (nc colour channels, maps or not).
 extern "C" cudaError_t rs_launch_wave_multi(const WaveArgs* jobs, int nreq, const int* prefix, int step, int visCur,

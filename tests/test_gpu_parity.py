@@ -298,11 +298,15 @@ def test_batch_matches_single_calls(oracle):
         single = R.image_synth(r["image"], r["mask"], r["fmt"], R.params(**r["params"]),
                                opts=R.options(mode=R.MODE_WAVEFRONT))
         assert single.rc == 0 and (single.out == out).all()
-    # one stream per request gives the same results with far more launches
+    # one stream per request, and the many-request path with one launch per
+    # step instead of one persistent launch per pass, give the same results
     rc2, outs2, codes2, st2 = R.image_synth_batch(items, opts=R.options(mode=R.MODE_WAVEFRONT, separateRequests=1),
                                                   concurrency=4)
     assert rc2 == 0 and all((a == b).all() for a, b in zip(outs, outs2))
-    assert st["launches"] < st2["launches"] / 2
+    rc3, outs3, codes3, st3 = R.image_synth_batch(items, opts=R.options(mode=R.MODE_WAVEFRONT, batchLaunches=1),
+                                                  concurrency=4)
+    assert rc3 == 0 and all((a == b).all() for a, b in zip(outs, outs3))
+    assert st["launches"] < st3["launches"] / 2
     # replay mode through the batch entry point is still byte-identical to the oracle
     rc, outs, codes, _ = R.image_synth_batch(items[:2], opts=R.options(mode=R.MODE_REPLAY), concurrency=2)
     assert rc == 0
