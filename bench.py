@@ -53,7 +53,7 @@ def term_ops(nc: int, nm: int) -> int:
 #   python bench.py --profile-once --no-cpu --warps 16 --workload W
 # ncu flushes the caches before each launch, so these are cold-cache figures:
 # an upper bound for the warm launches timed here.
-WAVE_DRAM_BYTES = {"render1024": 6.64e6, "heal4096": 67.63e6, "mapstyle2048": 28.58e6}
+WAVE_DRAM_BYTES = {}
 SAMPLE_SIDE = 256                 # CPU sample: 256x256 target from the same tile
 
 
@@ -317,7 +317,7 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
-def learned_comparison(size, train_images, train_pairs, train_steps, searches, reps=3):
+def learned_comparison(size, train_images, train_pairs, train_steps, searches, reps=3, pool=None):
     """Learned proposals against the plain search on the large-heal family
     (seeded value noise, union of 40 ellipses covering ~10 % of the image):
     pairs are dumped by plain wavefront runs over `train_images` images (seeds
@@ -349,8 +349,10 @@ def learned_comparison(size, train_images, train_pairs, train_steps, searches, r
     t0 = time.perf_counter()
     pairs = R.Pairs(train_pairs)
     per_image = max(1, train_pairs // train_images)
-    for i in range(1, train_images + 1):
-        wl = W.heal4096(index=i, size=size)
+    # training images (seeds 1..N) generated in spawned worker processes when a pool is given
+    images = (pool.imap(_cpu_job, [("heal", i, size) for i in range(1, train_images + 1)]) if pool else
+              (W.heal4096(index=i, size=size) for i in range(1, train_images + 1)))
+    for wl in images:
         run(wl, 200, dump=pairs, stride=max(1, wl["target_px"] // per_image), state=False)
     dump_s = time.perf_counter() - t0
     net = R.Net(seed=1)
@@ -389,28 +391,289 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ CPU helpers
+
+def cpu_engine(name: str, threads: int, want_energy: bool = True):
+    """The CPU engine (the reference built from its sources where present,
+    else its oracle port) on the whole workload `name`: (seconds, energy,
+    kind, output pixmap).  Energy = the full-patch metric summed over the
+    targets at their final sources, computed by the oracle's restatement of
+    computeBestFit (bit-exact with the GPU's resynthPatchEnergy)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    _, tgt, cor, spec, kw = load_workload(name)
+    o = O.Oracle()
+    fmt = o.format_indices(*spec)
+    p = O.make_params(**kw)
+    kind = "port"
+    t0 = time.perf_counter()
+    if O.reference_available(threaded=threads > 1):
+        rc, out, src, hv = O.Reference(threaded=threads > 1).engine_state(p, fmt, tgt, cor)
+        kind = "reference"
+    else:
+        rc, out, _, src, hv = o.engine(p, fmt, tgt, cor, threads=threads, want_state=True)
+    dt = time.perf_counter() - t0
+    assert rc == 0
+    e = None
+    if want_energy:
+        ys, xs = np.nonzero(tgt[..., 0] != 0)
+        targets = np.stack([xs, ys], 1).astype(np.int32)
+        e, _ = o.energy(p, fmt, out, cor, hv, src, targets)
+    return dt, e, kind, out
+
+
+def _cpu_job(job):
+    """Pool worker (spawned processes, never forked from the GPU process)."""
+    kind = job[0]
+    if kind == "engine":
+        dt, e, k, _ = cpu_engine(job[1], job[2])
+        return dt, e, k
+    from resynthesizer_gb300 import workloads as W
+    if kind == "batch":
+        return W.batch_request(job[1])
+    if kind == "heal":
+        return W.heal4096(index=job[1], size=job[2])
+    raise ValueError(kind)
+
+
+def spawn_pool(n: int):
+    import multiprocessing as mp
+    return mp.get_context("spawn").Pool(n)
+
+
+def cpu_reference_energies(name: str, mt_runs: int):
+    """The single-threaded engine once, alone (its time is the CPU baseline),
+    then `mt_runs` runs of the threaded engine (8 threads, nondeterministic)
+    side by side in spawned processes for their energies."""
+    st_s, st_e, kind, st_out = cpu_engine(name, 1)
+    mt = []
+    if mt_runs:
+        with spawn_pool(mt_runs) as pool:
+            mt = pool.map(_cpu_job, [("engine", name, 8)] * mt_runs)
+    return dict(st_seconds=st_s, st_energy=st_e, kind=kind, st_out=st_out,
+                mt_energies=[m[1] for m in mt], mt_seconds=[m[0] for m in mt])
+
+
+def energy_vs_reference(e_gpu: float, ref: dict) -> dict:
+    import numpy as np
+    mt = ref["mt_energies"]
+    mt_mean = float(np.mean(mt)) if mt else None
+    d = {"gpu_energy": e_gpu, "cpu_st_energy": ref["st_energy"], "gpu_over_st": e_gpu / ref["st_energy"],
+         "cpu_mt_energies": mt, "cpu_mt_mean": mt_mean,
+         "gpu_over_mt_mean": e_gpu / mt_mean if mt_mean else None,
+         "mt_spread": (max(mt) - min(mt)) / mt_mean if mt_mean else None,
+         "cpu_kind": ref["kind"],
+         "gate": "wavefront energy at most 1.01 x the threaded reference's mean (one-sided: lower is better)"}
+    if mt_mean:
+        d["gate_pass"] = bool(e_gpu <= 1.01 * mt_mean)
+    return d
+
+
+# ------------------------------------------------------------ reference arm
+
 def run_reference_arm(args):
+    """The reference's CPU engine on this machine's host cores, on the same
+    workload as the default GPU line (render1024, the whole 1024x1024 target
+    every step).  Its single-threaded build is the value: the threaded build
+    (THREAD_LIMIT 8 workers, lib/buildSwitches.h:89) serialises on a global
+    mutex and one shared rand() and runs about 5x slower on the same input
+    (one full-size run of it is reported beside).  Warm-up steps run a
+    256x256 sample; every timed step the full workload."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
-    # The reference's threaded engine (THREAD_LIMIT = 8 worker threads,
-    # lib/buildSwitches.h:89) on a bounded sample per step.
-    vals = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_sample(threads=8)
-        if i >= args.warmup:
-            vals.append(r)
-    total_px = SAMPLE_SIDE * SAMPLE_SIDE * len(vals)
-    total_s = sum(v["seconds"] for v in vals)
-    value = total_px / total_s
+    for _ in range(args.warmup):
+        cpu_sample(threads=1)
+    secs, kind = [], None
+    for _ in range(args.steps):
+        dt, _, kind, _ = cpu_engine("render1024", 1, want_energy=False)
+        secs.append(dt)
+    px = 1024 * 1024
+    value = px * len(secs) / sum(secs)
+    mt_s, _, mt_kind, _ = cpu_engine("render1024", 8, want_energy=False)
+    sample = "the whole workload (1024x1024 target) every timed step; single-threaded engine"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "target px/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total_s / len(vals),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(secs) / len(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": vals[0]["sample"], "threads": 8},
-            "cpu_baseline": {"value": value, "unit": "target px/s", "cores": 8, "kind": vals[0]["kind"],
-                             "sample": vals[0]["sample"]},
+            "config": {"workload": WORKLOAD, "target": "1024x1024", "corpus": "128x128", "target_px": px,
+                       "threads": 1, "same_config": True, "warmup_sample": "256x256 target from the same tile"},
+            "cpu_baseline": {"value": value, "unit": "target px/s", "cores": 1, "kind": kind, "sample": sample},
+            "threaded": {"value": px / mt_s, "unit": "target px/s", "threads": 8, "kind": mt_kind,
+                         "sample": "the whole workload, one run"},
             "e2e": {"value": value, "unit": "target px/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------- GPU measurements
+
+def device_timing(R, torch, wl: dict, opts, steps: int, warmup: int, flush, stream):
+    """engineDevice on pixmaps resident in device memory: per step a fresh
+    target copy and an L2 flush (outside the timed interval), then the
+    synthesis timed with CUDA events on the call's stream."""
+    dev = flush.device
+    tgt, cor = wl["target"], wl["corpus"]
+    th, tw, _ = tgt.shape
+    ch, cw, _ = cor.shape
+    t_init = torch.from_numpy(tgt).to(dev)
+    t_work = t_init.clone()
+    c_dev = torch.from_numpy(cor).to(dev)
+    p = R.params(**wl["params"])
+    fmt = R.format_indices(*wl["format"])
+    ms, stats = [], []
+    for i in range(warmup + steps):
+        t_work.copy_(t_init)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rc, st = R.engine_device(p, fmt, t_work.data_ptr(), tw, th, c_dev.data_ptr(), cw, ch,
+                                 stream=stream.cuda_stream, opts=opts)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if rc:
+            raise RuntimeError(f"engineDevice rc={rc}: {R.last_error()}")
+        if i >= warmup:
+            ms.append(e0.elapsed_time(e1))
+            stats.append(st)
+    return ms, stats
+
+
+def e2e_engine(R, wl: dict, opts, steps: int, warmup: int):
+    """engineEx on host Maps (the reference's engine() call with options):
+    host->device copies, synthesis and the device->host copy of the target,
+    wall-clock timed around the C call."""
+    L = R.lib()
+    p = R.params(**wl["params"])
+    fmt = R.format_indices(*wl["format"])
+    ms, h2d, d2h = [], 0, 0
+    for i in range(warmup + steps):
+        tm, cm = R.PixmapMap(wl["target"]), R.PixmapMap(wl["corpus"])
+        stt = R.Stats()
+        t0 = time.perf_counter()
+        rc = L.engineEx(R.C.byref(p), R.C.byref(fmt), R.C.byref(tm.map), R.C.byref(cm.map), None, None, None,
+                        R.C.byref(opts), R.C.byref(stt))
+        dt = time.perf_counter() - t0
+        assert rc == 0, R.last_error()
+        if i >= warmup:
+            ms.append(dt * 1000)
+            h2d, d2h = stt.h2dBytes, stt.d2hBytes
+    return ms, h2d, d2h
+
+
+def e2e_image_synth(R, image, mask, fmt: int, params: dict, opts, steps: int, warmup: int):
+    """imageSynthEx on the caller's row buffers (the reference's imageSynth
+    call with options), wall-clock timed around the C call; the image is
+    restored between calls outside the timed interval."""
+    import numpy as np
+    L = R.lib()
+    p = R.params(**params)
+    img = np.ascontiguousarray(image).copy()
+    m = np.ascontiguousarray(mask)
+    ib, mb = R._buf(img), R._buf(m)
+    cf = R.C.c_int(0)
+    ms, h2d, d2h = [], 0, 0
+    for i in range(warmup + steps):
+        img[...] = image
+        st = R.Stats()
+        t0 = time.perf_counter()
+        rc = L.imageSynthEx(R.C.byref(ib), R.C.byref(mb), None, fmt, R.C.byref(p), None, None, R.C.byref(cf),
+                            R.C.byref(opts), R.C.byref(st))
+        dt = time.perf_counter() - t0
+        assert rc == 0, R.last_error()
+        if i >= warmup:
+            ms.append(dt * 1000)
+            h2d, d2h = st.h2dBytes, st.d2hBytes
+    return ms, h2d, d2h, img
+
+
+def gpu_energy(R, wl: dict, out, has_value, source):
+    import numpy as np
+    sel = wl["target"][..., 0] != 0
+    ys, xs = np.nonzero(sel)
+    targets = np.stack([xs, ys], 1).astype(np.int32)
+    e, _ = R.patch_energy(R.params(**wl["params"]), R.format_indices(*wl["format"]), out, wl["corpus"], has_value,
+                          source, targets)
+    return e
+
+
+def workload_dict(name: str) -> dict:
+    wname, t, c, spec, kw = load_workload(name)
+    return {"name": wname, "target": t, "corpus": c, "format": spec, "params": kw,
+            "target_px": int((t[..., 0] != 0).sum())}
+
+
+def sub_line(R, torch, name, flush, stream, steps=5, warmup=2, pool=None, mt_runs=0):
+    """Figures of one more workload of the survey's set, all outside the
+    main line's timed region: device-resident and end-to-end px/s, energy,
+    and -- where the CPU engine finishes in seconds -- its energy beside."""
+    import numpy as np
+    from resynthesizer_gb300 import workloads as W
+    t0 = time.perf_counter()
+    wl = workload_dict(name)
+    gen_s = time.perf_counter() - t0
+    opts = R.options(mode=R.MODE_WAVEFRONT)
+    ms, stats = device_timing(R, torch, wl, opts, steps, warmup, flush, stream)
+    d = {"workload": name, "target_px": wl["target_px"], "generation_s": gen_s,
+         "device_px_per_s": wl["target_px"] / (min(ms) / 1000.0), "device_ms": ms,
+         "evals_per_s": stats[0]["evals"] / (min(ms) / 1000.0), "passes": stats[0]["passes"],
+         "launches": stats[0]["launches"]}
+    if name.startswith("heal"):
+        heal = W.heal256() if name == "heal256" else W.heal4096()
+        ems, h2d, d2h, _ = e2e_image_synth(R, heal["image"], heal["mask"], heal["fmt"], heal["params"], opts, steps,
+                                           warmup)
+        d["e2e"] = {"value": wl["target_px"] / (np.median(ems) / 1000.0), "unit": "target px/s",
+                    "call": "imageSynthEx on host row buffers", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h}
+    else:
+        ems, h2d, d2h = e2e_engine(R, wl, opts, steps, warmup)
+        d["e2e"] = {"value": wl["target_px"] / (np.median(ems) / 1000.0), "unit": "target px/s",
+                    "call": "engineEx on host Maps", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    res = R.engine(wl["target"], wl["corpus"], R.format_indices(*wl["format"]), R.params(**wl["params"]),
+                   opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1))
+    e = gpu_energy(R, wl, res.out, res.has_value, res.source)
+    d["energy_per_px"] = e / wl["target_px"]
+    if mt_runs:
+        ref = cpu_reference_energies(name, mt_runs)
+        d["energy_vs_reference"] = energy_vs_reference(e, ref)
+        d["cpu_single_thread_px_per_s"] = wl["target_px"] / ref["st_seconds"]
+        if name == "heal256":
+            r = R.engine(wl["target"], wl["corpus"], R.format_indices(*wl["format"]), R.params(**wl["params"]),
+                         opts=R.options(mode=R.MODE_REPLAY))
+            d["replay"] = {"ms": r.stats["deviceMs"], "identical_to_cpu_single_thread":
+                           bool(r.rc == 0 and np.array_equal(r.out, ref["st_out"]))}
+    else:
+        d["energy_vs_reference"] = ("not run here: the CPU engine needs minutes at this size "
+                                    "(its offline figure is in the design notes)")
+    return d
+
+
+def batch_line(R, n: int, pool, steps=2):
+    """Batched heal requests through imageSynthBatch with host buffers."""
+    from resynthesizer_gb300 import workloads as W
+    t0 = time.perf_counter()
+    specs = W.batch_specs(n=n)
+    reqs = pool.map(_cpu_job, [("batch", sp) for sp in specs], chunksize=4) if pool else \
+        [W.batch_request(sp) for sp in specs]
+    gen_s = time.perf_counter() - t0
+    items = [(r["image"], r["mask"], r["fmt"], R.params(**r["params"])) for r in reqs]
+    px = sum(r["target_px"] for r in reqs)
+    opts = R.options(mode=R.MODE_WAVEFRONT)
+    rc, _, _, _ = R.image_synth_batch(items[:16], opts=opts)
+    assert rc == 0, R.last_error()
+    ts, st = [], None
+    for _ in range(steps):
+        t1 = time.perf_counter()
+        rc, _, codes, st = R.image_synth_batch(items, opts=opts)
+        ts.append(time.perf_counter() - t1)
+        assert rc == 0, R.last_error()
+    return {"workload": f"batch{n}: {n} heal requests, 128..1024 px sides, Gray/RGB/RGBA, holes 2-20 %, "
+                        f"P in {{9,16,30}}, trys=200, imageSynthBatch", "requests": n, "target_px": px,
+            "generation_s": gen_s, "e2e": {"value": px / min(ts), "unit": "target px/s",
+                                           "call": "imageSynthBatch on host row buffers (wall clock)",
+                                           "h2d_bytes_per_step": st["h2dBytes"], "d2h_bytes_per_step": st["d2hBytes"]},
+            "ms": [1000 * t for t in ts], "launches": st["launches"], "device_ms": st["deviceMs"],
+            "evals_per_s": st["evals"] / min(ts)}
 
 
 def main():
@@ -419,16 +682,21 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines and energies")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="only the main line (no other workloads, no learned comparison)")
     ap.add_argument("--warps", type=int, default=0,
                     help="warps per CTA of the synthesis kernel (0 = autotuned; fix it when profiling, since the "
                          "tuner's timings are not meaningful under a profiler)")
     ap.add_argument("--profile-once", action="store_true",
                     help="one warm-up and one timed engineDevice call only (for ncu captures)")
+    ap.add_argument("--batch-launches", action="store_true",
+                    help="one kernel launch per batch instead of one persistent launch per pass")
     ap.add_argument("--workload", default="render1024",
-                    help="render1024 (default), heal256, heal4096, mapstyle2048")
+                    help="render1024 (default), heal256, heal4096, mapstyle2048, batchN")
     ap.add_argument("--quality", action="store_true", help="energy against the CPU engine instead of speed")
     ap.add_argument("--quality-runs", type=int, default=3)
+    ap.add_argument("--mt-runs", type=int, default=3, help="threaded CPU runs for the energy gate")
     ap.add_argument("--concurrency", type=int, default=8, help="host workers for batch workloads")
     ap.add_argument("--learned", action="store_true", help="learned proposals against the plain search")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain object of the bench line")
@@ -458,7 +726,6 @@ def main():
 
     import resynthesizer_gb300 as R
     from resynthesizer_gb300 import build as B
-    from resynthesizer_gb300 import workloads as W
 
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
@@ -469,95 +736,77 @@ def main():
         B.build()
     if world > 1:
         dist.barrier()
-    L = R.lib()
 
-    wname, w_target, w_corpus, w_spec, w_params = load_workload(args.workload)
-    wl = {"target": w_target, "corpus": w_corpus, "format": w_spec, "params": w_params}
+    wl = workload_dict(args.workload)
+    wname = wl["name"]
     p = R.params(**wl["params"])
     fmt = R.format_indices(*wl["format"])
     th, tw, _ = wl["target"].shape
     ch, cw, _ = wl["corpus"].shape
-    target_px = int((wl["target"][..., 0] != 0).sum())
+    target_px = wl["target_px"]
     dev = torch.device("cuda", local)
-    t_init = torch.from_numpy(wl["target"]).to(dev)
-    t_work = t_init.clone()
-    c_dev = torch.from_numpy(wl["corpus"]).to(dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > 129 MB L2
     stream = torch.cuda.current_stream()
-    opts = R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=args.warps)
-
-    def step(o=opts):
-        t_work.copy_(t_init)
-        rc, st = R.engine_device(p, fmt, t_work.data_ptr(), tw, th, c_dev.data_ptr(), cw, ch,
-                                 stream=stream.cuda_stream, opts=o)
-        if rc:
-            raise RuntimeError(f"engineDevice rc={rc}: {R.last_error()}")
-        return st
+    opts = R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=args.warps, batchLaunches=int(args.batch_launches))
 
     if args.profile_once:
-        step()
-        torch.cuda.synchronize()
-        st = step()
-        torch.cuda.synchronize()
-        print(json.dumps({"profile_once": True, "stats": st}), flush=True)
+        ms, stats = device_timing(R, torch, wl, opts, 1, 1, flush, stream)
+        print(json.dumps({"profile_once": True, "ms": ms, "stats": stats[0]}), flush=True)
         return
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+    device_timing(R, torch, wl, opts, 0, args.warmup, flush, stream)
     if world > 1:
         dist.barrier()
 
-    # device-resident throughput
-    ms, evals, launches = [], 0, 0
+    # device-resident throughput (the timed region)
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            st = step()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-            evals += st["evals"]
-            launches += st["launches"]
+        ms, stats = device_timing(R, torch, wl, opts, args.steps, 0, flush, stream)
     total_ms = max_over_ranks(sum(ms), dev)
     if world > 1:
         dist.barrier()
     value = replica_throughput(world, args.steps, target_px, total_ms)
-    evals_per_s = world * evals / (total_ms / 1000.0)
+    evals_per_s = world * sum(s["evals"] for s in stats) / (total_ms / 1000.0)
+    launches = sum(s["launches"] for s in stats)
 
     # end to end through the reference-facing call with host buffers
-    e2e_ms, h2d, d2h = [], 0, 0
-    for i in range(args.warmup + args.steps):
-        tm, cm = R.PixmapMap(wl["target"]), R.PixmapMap(wl["corpus"])
-        stt = R.Stats()
-        t0 = time.perf_counter()
-        rc = L.engineEx(R.C.byref(p), R.C.byref(fmt), R.C.byref(tm.map), R.C.byref(cm.map), None, None, None,
-                        R.C.byref(opts), R.C.byref(stt))
-        dt = time.perf_counter() - t0
-        assert rc == 0, R.last_error()
-        if i >= args.warmup:
-            e2e_ms.append(dt * 1000)
-            h2d, d2h = stt.h2dBytes, stt.d2hBytes
+    e2e_ms, h2d, d2h = e2e_engine(R, wl, opts, args.steps, args.warmup)
     e2e_value = world * args.steps * target_px / (sum(e2e_ms) / 1000.0)
 
-    # dominant kernel: the per-target synthesis launches, timed live
-    flush.fill_(1)
-    torch.cuda.synchronize()
-    prof = step(R.options(mode=R.MODE_WAVEFRONT, profile=1, warpsPerBlock=args.warps))
+    # dominant kernel: the wavefront synthesis launches, timed live with CUDA
+    # events on the library's stream, against the two on-chip peaks that
+    # bound it (measured here) and, as a secondary figure, the HBM copy peak
+    _, pst = device_timing(R, torch, wl, R.options(mode=R.MODE_WAVEFRONT, profile=1, warpsPerBlock=args.warps,
+                                                   batchLaunches=int(args.batch_launches)), 1, 0, flush, stream)
+    prof = pst[0]
     wave_ms_per_launch = prof["waveMs"] / max(1, prof["waveLaunches"])
     terms_per_launch = prof["waveTerms"] / max(1, prof["waveLaunches"])
     tb, to = term_bytes(fmt.img_match_bpp, fmt.map_match_bpp), term_ops(fmt.img_match_bpp, fmt.map_match_bpp)
-    achieved_gbs = terms_per_launch * tb / (wave_ms_per_launch / 1000.0) / 1e9
-    peak, peak_kind = peaks()
+    smem_peak, _ = R.microbench(0)
+    int_peak, _ = R.microbench(1)
+    hbm_peak, hbm_kind = peaks()
+    sec = wave_ms_per_launch / 1000.0
+    smem_gbs = terms_per_launch * tb / sec / 1e9
+    int_gops = terms_per_launch * to / sec / 1e9
+    fr = {"smem": smem_gbs / smem_peak, "int32": int_gops / int_peak}
+    bound = max(fr, key=fr.get)
+    roof = {"bound": bound, "achieved": smem_gbs if bound == "smem" else int_gops,
+            "peak": smem_peak if bound == "smem" else int_peak, "unit": "GB/s" if bound == "smem" else "G int ops/s",
+            "frac": fr[bound], "traffic": WAVE_DRAM_BYTES.get(wname), "kernel": "k_wave_persistent",
+            "peak_source": "measured in this run: resynthMicrobench (conflict-free 16-byte shared loads; chains of "
+                           "32-bit add and xor), best of five CUDA-event-timed launches",
+            "smem": {"achieved": smem_gbs, "peak": smem_peak, "unit": "GB/s", "frac": fr["smem"],
+                     "bytes_per_term": tb},
+            "int32": {"achieved": int_gops, "peak": int_peak, "unit": "G ops/s", "frac": fr["int32"],
+                      "ops_per_term": to},
+            "hbm": {"achieved": smem_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": smem_gbs / hbm_peak,
+                    "peak_kind": hbm_kind, "note": "algorithmic bytes over the HBM copy peak; the corpus and "
+                                                  "tables are read from shared memory and L1, DRAM traffic is the "
+                                                  "'traffic' figure"},
+            "launches": prof["waveLaunches"], "ms_per_launch": wave_ms_per_launch,
+            "terms_per_launch": terms_per_launch}
 
     # quality of this run (outside every timed region)
     res = R.engine(wl["target"], wl["corpus"], fmt, p, opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1))
-    sel = wl["target"][..., 0] != 0
-    ys, xs = np.nonzero(sel)
-    targets = np.stack([xs, ys], 1).astype(np.int32)
-    energy, _ = R.patch_energy(p, fmt, res.out, wl["corpus"], res.has_value, res.source, targets)
+    energy = gpu_energy(R, wl, res.out, res.has_value, res.source)
 
     if rank != 0:
         return
@@ -567,6 +816,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": WORKLOAD if wname == "render1024" else wname, "target": f"{tw}x{th}",
                    "corpus": f"{cw}x{ch}", "target_px": target_px, "mode": "wavefront",
+                   "launch": "one launch per batch" if args.batch_launches else "one persistent launch per pass",
                    "l2": "flushed (256 MB write) between steps, outside the timed intervals",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "evals_per_s": evals_per_s,
@@ -574,34 +824,43 @@ def main():
         "passes": res.stats["passes"],
         "gpu_launches": launches,
         "e2e": {"value": e2e_value, "unit": "target px/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
-                     "frac": achieved_gbs / peak, "traffic": WAVE_DRAM_BYTES.get(wname), "kernel": "k_wave",
-                     "peak_kind": peak_kind, "launches": prof["waveLaunches"],
-                     "ms_per_launch": wave_ms_per_launch, "terms_per_launch": terms_per_launch,
-                     "bytes_per_term": tb, "int_ops_per_s": terms_per_launch * to /
-                     (wave_ms_per_launch / 1000.0)},
+        "roofline": roof,
         "clocks": clk.summary(),
     }
     if not args.no_cpu and wname == "render1024":
-        mt = cpu_sample(threads=8)
-        stt = cpu_sample(threads=1)
-        line["cpu_baseline"] = {"value": mt["value"], "unit": "target px/s", "cores": 8, "kind": mt["kind"],
-                                "sample": mt["sample"], "single_thread_value": stt["value"]}
+        ref = cpu_reference_energies("render1024", args.mt_runs)
+        line["cpu_baseline"] = {"value": target_px / ref["st_seconds"], "unit": "target px/s", "cores": 1,
+                                "kind": ref["kind"], "sample": "the whole workload (1024x1024 target), one run of "
+                                                              "the single-threaded engine"}
+        line["energy_vs_reference"] = energy_vs_reference(energy, ref)
+        line["energy_vs_reference"]["psnr_vs_cpu_st"] = psnr(res.out[..., 1:4], ref["st_out"][..., 1:4])
         try:
             line["cpu_same_schedule"] = cpu_same_schedule(wl["target"], wl["corpus"], wl["format"], wl["params"],
                                                           res.out, min(16, os.cpu_count() or 1))
         except Exception as e:   # an informative extra: never fails the bench line
             line["cpu_same_schedule"] = {"error": repr(e)[:200]}
-    if not args.no_learned and wname == "render1024" and rank == 0:
-        # learned vs plain (outside every timed region above): a 1024^2 heal,
-        # network trained on pairs from four plain runs, 200 probes each way
-        c = learned_comparison(1024, 4, 400000, 1000, [(200, False), (200, True)])
-        plain, learned = c["rows"]
-        line["learned"] = {"workload": "heal1024: seeded value noise, 40 ellipses ~10 %, P=30, trys=200",
-                           "train": {"images": 4, "pairs": c["train_pairs"], "steps": 1000, "seconds": c["train_s"]},
-                           "plain_px_per_s": plain["px_per_s"], "learned_px_per_s": learned["px_per_s"],
-                           "learned_vs_plain_px_per_s": learned["px_per_s"] / plain["px_per_s"],
-                           "learned_energy_vs_plain": learned["energy"] / plain["energy"]}
+    if not args.no_extra and wname == "render1024":
+        extra = {}
+        with spawn_pool(min(16, os.cpu_count() or 1)) as pool:
+            for name in ("heal256", "heal4096", "mapstyle2048"):
+                try:
+                    extra[name] = sub_line(R, torch, name, flush, stream,
+                                           mt_runs=0 if (args.no_cpu or name != "heal256") else 5)
+                except Exception as e:
+                    extra[name] = {"error": repr(e)[:300]}
+            try:
+                extra["batch512"] = batch_line(R, 512, pool)
+            except Exception as e:
+                extra["batch512"] = {"error": repr(e)[:300]}
+            if not args.no_learned:
+                try:
+                    extra["learned_heal4096"] = learned_comparison(4096, 64, 2000000, 4000,
+                                                                   [(200, False), (64, False), (16, False),
+                                                                    (200, True), (64, True), (16, True)], reps=2,
+                                                                   pool=pool)
+                except Exception as e:
+                    extra["learned_heal4096"] = {"error": repr(e)[:300]}
+        line["workloads"] = extra
     print(json.dumps(line), flush=True)
 
 

@@ -1093,6 +1093,15 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+// A poll that neither caches the line in L1 nor invalidates L1 (an acquire
+// load would, on every poll, taking the L1 away from a working CTA on the
+// same SM); the acquire fence comes once, after the value changed.
+__device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -1127,13 +1136,16 @@ __device__ bool grid_barrier(GridBar* gb, const volatile int* abortFlag, unsigne
     } else {
       const unsigned long long t0 = global_ns();
       bool late = false;
-      while (ld_acquire_gpu(&gb->gen) == gen) {
+      unsigned nap = 32;
+      while (ld_relaxed_gpu(&gb->gen) == gen) {
         if ((long long)(global_ns() - t0) > timeoutNs) {
           late = true;
           break;
         }
-        __nanosleep(64);
+        __nanosleep(nap);
+        if (nap < 256) nap <<= 1;
       }
+      fence_acq_rel_gpu();
       if (late) {
         atomicOr(err, kErrBarrier);
         stop = 1u;

@@ -241,24 +241,38 @@ def heal4096(index: int = 0, size: int = 4096) -> dict:
                 target_px=int((mask > 0).sum()))
 
 
-def batch_requests(n: int = 512, lo: int = 128, hi: int = 1024, index: int = 0) -> list[dict]:
+def batch_specs(n: int = 512, lo: int = 128, hi: int = 1024, index: int = 0) -> list[dict]:
+    """The per-request draws of batch_requests (size, layout, hole fraction,
+    patch size), in request order; batch_request() makes one request's images
+    from its spec, so requests can be generated in parallel."""
     rng = SplitMix64(1000 * 3 + index)
-    reqs = []
+    specs = []
     for r in range(n):
         w, h = (int(v) for v in rng.integers(2, lo, hi))
         fmt = [T_Gray, T_RGB, T_RGBA][int(rng.integers(1, 0, 2)[0])]
-        frac = rng.uniform(1, 0.02, 0.20)[0]
+        frac = float(rng.uniform(1, 0.02, 0.20)[0])
         patch = [9, 16, 30][int(rng.integers(1, 0, 2)[0])]
-        sub = SplitMix64(1000 * 3 + 7919 * (r + 1) + index)
-        img = value_noise_separable(h, w, PIXELELS[fmt], sub)
-        if fmt == T_RGBA:
-            img[..., 3] = 255
-        rmax = max(8.0, 0.25 * min(w, h))
-        mask = ellipse_mask_fast(h, w, sub, 1 + int(frac * 40), 4.0, rmax, frac * 0.8, frac * 1.25, rects=True)
-        reqs.append(dict(name=f"req{r}", image=img, mask=mask, fmt=fmt,
-                         params=dict(matchContextType=1, patchSize=patch, maxProbeCount=200, sensitivity=0.117),
-                         target_px=int((mask > 0).sum())))
-    return reqs
+        specs.append(dict(r=r, w=w, h=h, fmt=fmt, frac=frac, patch=patch, index=index))
+    return specs
+
+
+def batch_request(spec: dict) -> dict:
+    r, w, h, fmt, frac, index = spec["r"], spec["w"], spec["h"], spec["fmt"], spec["frac"], spec["index"]
+    sub = SplitMix64(1000 * 3 + 7919 * (r + 1) + index)
+    img = value_noise_separable(h, w, PIXELELS[fmt], sub)
+    if fmt == T_RGBA:
+        img[..., 3] = 255
+    rmax = max(8.0, 0.25 * min(w, h))
+    mask = ellipse_mask_fast(h, w, sub, 1 + int(frac * 40), 4.0, rmax, frac * 0.8, frac * 1.25, rects=True)
+    return dict(name=f"req{r}", image=img, mask=mask, fmt=fmt,
+                params=dict(matchContextType=1, patchSize=spec["patch"], maxProbeCount=200, sensitivity=0.117),
+                target_px=int((mask > 0).sum()))
+
+
+def batch_requests(n: int = 512, lo: int = 128, hi: int = 1024, index: int = 0) -> list[dict]:
+    """Batched heal requests: sizes uniform in lo..hi per side, Gray/RGB/RGBA,
+    holes of random ellipses and rectangles covering 2-20 %, P in {9, 16, 30}."""
+    return [batch_request(sp) for sp in batch_specs(n, lo, hi, index)]
 
 
 def gaussian_blur(a: np.ndarray, sigma: float) -> np.ndarray:
