@@ -1035,17 +1035,34 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
         }
         if (tuning && b == 2) CK(cudaEventRecord(tev[3], s));
       }
-      // the rest of the pass, after the single launches it depends on
+      // The rest of the pass, after the single launches it depends on.  A
+      // launch's grid fits its bands: a band's batches want about twice their
+      // expected size in CTAs (one team per target, with slack for the
+      // spread), so runs of consecutive bands are grouped into grid classes
+      // of at most 32 CTAs, at most 128, and the whole GPU.  Small pass-0
+      // bands then meet at barriers of few CTAs; large ones use every SM.
       if (persistent && singleEnd < nbatches) {
-        wa.batch = singleEnd;
-        wa.batchEnd = nbatches;
+        auto gridClass = [&](int b) {
+          const int band = b / (k * k);
+          const long long count = bandEnds[band] - (band ? bandEnds[band - 1] : 0);
+          const long long want = 2 * ((count + k * k - 1) / (k * k)) + 4;
+          return want <= 32 ? 32 : want <= 128 ? 128 : 0;
+        };
         wa.gbar = gbar;
         wa.barTimeoutNs = kBarrierTimeoutNs;
-        CK(cudaMemsetAsync(gbar, 0, sizeof(rs::GridBar), s));
-        if (opt.profile) prof.begin(s);
-        CK(rs_launch_wave_persistent(wa, warps, s));
-        if (opt.profile) prof.end(s);
-        launches += 2;
+        for (int b = singleEnd; b < nbatches;) {
+          const int cls = gridClass(b);
+          int e = b + 1;
+          while (e < nbatches && gridClass(e) == cls) e++;
+          wa.batch = b;
+          wa.batchEnd = e;
+          CK(cudaMemsetAsync(gbar, 0, sizeof(rs::GridBar), s));
+          if (opt.profile) prof.begin(s);
+          CK(rs_launch_wave_persistent(wa, warps, cls, s));
+          if (opt.profile) prof.end(s);
+          launches += 2;
+          b = e;
+        }
       }
       cudaGraphExec_t passExec = nullptr;
       if (graphPass) {

@@ -145,8 +145,9 @@ cudaError_t rs_launch_unpack_colors(uint8_t* raw, int w, int h, int bpp, int nc,
 cudaError_t rs_launch_replay(const rs::ReplayArgs& a, int t0, int t1, cudaStream_t s);
 cudaError_t rs_launch_wave(const rs::WaveArgs& a, int warpsPerBlock, int maxCtas, cudaStream_t s);
 cudaError_t rs_launch_commit(const rs::WaveArgs& a, int maxCtas, cudaStream_t s);
-// Batches a.batch .. a.batchEnd - 1 of one problem in one cooperative launch.
-cudaError_t rs_launch_wave_persistent(const rs::WaveArgs& a, int warpsPerBlock, cudaStream_t s);
+// Batches a.batch .. a.batchEnd - 1 of one problem in one cooperative launch
+// of at most maxCtas CTAs (0 = one per resident slot of the GPU).
+cudaError_t rs_launch_wave_persistent(const rs::WaveArgs& a, int warpsPerBlock, int maxCtas, cudaStream_t s);
 // Whether this device can run the persistent kernel (cooperative launches).
 int rs_persistent_supported();
 int rs_wave_corpus_staged(const rs::Problem& pb, int warps);

@@ -1749,7 +1749,7 @@ extern "C" cudaError_t rs_launch_wave(const WaveArgs& a, int warps, int maxCtas,
 
 namespace {
 template <int NC, bool MAP, bool SMEMC>
-cudaError_t launch_wave_persistent_t(const WaveArgs& a, int warps, size_t smem, cudaStream_t s) {
+cudaError_t launch_wave_persistent_t(const WaveArgs& a, int warps, int maxCtas, size_t smem, cudaStream_t s) {
   auto kern = k_wave_persistent<NC, MAP, SMEMC>;
   static std::mutex mu;
   static size_t configured = 0;
@@ -1779,11 +1779,13 @@ cudaError_t launch_wave_persistent_t(const WaveArgs& a, int warps, size_t smem, 
   // barrier needs (the cooperative launch refuses a grid that could not be).
   WaveArgs args = a;
   void* params[] = {&args};
-  return cudaLaunchCooperativeKernel((const void*)kern, dim3(sm_count() * perSm), dim3(warps * 32), params, smem, s);
+  int grid = sm_count() * perSm;
+  if (maxCtas > 0) grid = std::min(grid, maxCtas);
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(warps * 32), params, smem, s);
 }
 }  // namespace
 
-extern "C" cudaError_t rs_launch_wave_persistent(const WaveArgs& a, int warps, cudaStream_t s) {
+extern "C" cudaError_t rs_launch_wave_persistent(const WaveArgs& a, int warps, int maxCtas, cudaStream_t s) {
   if (warps < 1) warps = 16;
   if (warps > 16) warps = 16;
   const size_t smemCorpus = wave_smem(a.pb, true, warps);
@@ -1791,9 +1793,9 @@ extern "C" cudaError_t rs_launch_wave_persistent(const WaveArgs& a, int warps, c
   const size_t smem = smemc ? smemCorpus : wave_smem(a.pb, false, warps);
   cudaError_t e = cudaSuccess;
   if (smemc) {
-    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_persistent_t<NC, MAP, true>(a, warps, smem, s)));
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_persistent_t<NC, MAP, true>(a, warps, maxCtas, smem, s)));
   } else {
-    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_persistent_t<NC, MAP, false>(a, warps, smem, s)));
+    RS_DISPATCH(a.pb.nc, a.pb.nm > 0, (e = launch_wave_persistent_t<NC, MAP, false>(a, warps, maxCtas, smem, s)));
   }
   return e;
 }
