@@ -2,7 +2,8 @@
 # build_ref.sh -- compile the reference engine from its own sources, in place,
 # into oracle/_ref/ (git-ignored).  TEST INFRASTRUCTURE ONLY.
 #
-# Usage: sh oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: sh oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT: the argument, else $RESYNTH_REFERENCE_ROOT, else /root/reference
 #
 # Outputs:
 #   oracle/_ref/libref_st.so   single-threaded engine (the bit-exact oracle pin)
@@ -16,7 +17,7 @@
 # searching the including file's own directory first.  Nothing under the
 # reference tree is modified or copied.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${RESYNTH_REFERENCE_ROOT:-/root/reference}}
 LIB="$REF/lib"
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"

@@ -21,6 +21,16 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "lib", "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
+# Where the reference tree is read from (its sources are compiled in place by
+# build_ref.sh): the environment variable RESYNTH_REFERENCE_ROOT, else the
+# location build_ref.sh uses by default.  Where it does not exist (a machine
+# without the reference), everything that needs it is skipped.
+REFERENCE_ROOT = os.environ.get("RESYNTH_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_tree() -> str | None:
+    """The reference tree's root if its engine sources are there, else None."""
+    return REFERENCE_ROOT if os.path.exists(os.path.join(REFERENCE_ROOT, "lib", "engine.c")) else None
 
 
 class Params(C.Structure):

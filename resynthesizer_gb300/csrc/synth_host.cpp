@@ -888,6 +888,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     const bool sparseOk = noContext && !dp.pb.tileH && !dp.pb.tileV;
     wa.stageSrc = ar.alloc<int2>(ntargets);
     rs::GridBar* gbar = ar.alloc<rs::GridBar>(1);
+    unsigned* dQueue = ar.alloc<unsigned>((size_t)kMaxBands * k * k);
     int2* dPass = ar.alloc<int2>(ntargets);
     int* dBandEnds = ar.alloc<int>(kMaxBands);
     int* dBandPhased = ar.alloc<int>(kMaxBands);
@@ -1056,11 +1057,13 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
           while (e < nbatches && gridClass(e) == cls) e++;
           wa.batch = b;
           wa.batchEnd = e;
+          wa.queue = dQueue;
           CK(cudaMemsetAsync(gbar, 0, sizeof(rs::GridBar), s));
+          CK(cudaMemsetAsync(dQueue + b, 0, (size_t)(e - b) * sizeof(unsigned), s));
           if (opt.profile) prof.begin(s);
           CK(rs_launch_wave_persistent(wa, warps, cls, s));
           if (opt.profile) prof.end(s);
-          launches += 2;
+          launches++;
           b = e;
         }
       }

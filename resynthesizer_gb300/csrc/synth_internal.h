@@ -115,6 +115,7 @@ struct WaveArgs {
   // with a grid barrier after each, and a commit phase between barriers when
   // results are staged):
   int batchEnd;
+  unsigned int* queue;           // per batch: next slot to hand out (zeroed by the host), or null = static shares
   GridBar* gbar;
   long long barTimeoutNs;        // a barrier wait longer than this gives up (kErrBarrier)
 };

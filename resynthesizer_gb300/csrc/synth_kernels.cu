@@ -1219,7 +1219,7 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
   }
   load_half_tables(pb, ct, mt);
   __shared__ unsigned long long s_key[16];
-  __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16];
+  __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16], s_item[16];
   __shared__ unsigned s_better;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
@@ -1239,9 +1239,31 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
       const WaveTeam T{G, team, warp % G, team * G, lane, warp, p, s_key, s_n, s_np, s_fast, s_gather};
       const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
       const int visCur = a.pass == 0 ? b : 0x7ffffffe;
-      for (int slot = blockIdx.x * teamsPerBlock + team; slot < nslots; slot += gridDim.x * teamsPerBlock) {
-        const unsigned better = wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
-        if (better) atomicAdd(&s_better, 1u);
+      if (a.queue && !a.probeShare) {
+        // Slots handed out one at a time from the batch's queue: a team takes
+        // the next slot as soon as it is done (its next grab is in flight
+        // while it works), so the batch ends when its last target does, not
+        // when the team with the slowest share does.
+        if (T.tw == 0 && lane == 0) s_item[team] = (int)atomicAdd(&a.queue[b], 1u);
+        T.sync();
+        int slot = s_item[team];
+        while (slot < nslots) {
+          int nxt = 0;
+          if (T.tw == 0 && lane == 0) nxt = (int)atomicAdd(&a.queue[b], 1u);
+          const unsigned better = wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
+          if (better) atomicAdd(&s_better, 1u);
+          if (T.tw == 0 && lane == 0) s_item[team] = nxt;
+          T.sync();
+          slot = s_item[team];
+        }
+      } else {
+        // Probes shared by groups of 16 slots: the warps of a CTA take 16
+        // consecutive slots together, so they read the same corpus windows.
+        for (int slot = blockIdx.x * teamsPerBlock + team; slot < nslots; slot += gridDim.x * teamsPerBlock) {
+          const unsigned better =
+              wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
+          if (better) atomicAdd(&s_better, 1u);
+        }
       }
     }
     if (!a.inPlace) {

@@ -100,8 +100,9 @@ def test_format_and_map_helpers(lib):
 def test_reference_testsynth_links_unchanged(lib, tmp_path):
     """The reference's own test harness, compiled against the reference's
     headers, links against this library with no source change."""
-    ref = "/root/reference"
-    if not os.path.exists(os.path.join(ref, "src", "testSynth.c")):
+    from oracle import reference_tree
+    ref = reference_tree()
+    if not ref or not os.path.exists(os.path.join(ref, "src", "testSynth.c")):
         pytest.skip("reference tree not present")
     shim = tmp_path / "shim"
     shim.mkdir()
