@@ -1240,16 +1240,25 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
       const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
       const int visCur = a.pass == 0 ? b : 0x7ffffffe;
       if (a.queue && !a.probeShare) {
-        // Slots handed out one at a time from the batch's queue: a team takes
-        // the next slot as soon as it is done (its next grab is in flight
-        // while it works), so the batch ends when its last target does, not
-        // when the team with the slowest share does.
-        if (T.tw == 0 && lane == 0) s_item[team] = (int)atomicAdd(&a.queue[b], 1u);
+        // Three quarters of the batch in fixed shares -- the teams of a CTA
+        // take neighbouring slots, whose patches overlap in L1 -- then the
+        // rest handed out one slot at a time from the batch's queue, so that
+        // the batch ends when its last target does rather than when the team
+        // with the slowest share does.  (A team's next grab is in flight
+        // while it works.)
+        const int stride = gridDim.x * teamsPerBlock;
+        const int fixedEnd = (nslots * 3 / 4) / stride * stride;
+        for (int slot = blockIdx.x * teamsPerBlock + team; slot < fixedEnd; slot += stride) {
+          const unsigned better =
+              wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
+          if (better) atomicAdd(&s_better, 1u);
+        }
+        if (T.tw == 0 && lane == 0) s_item[team] = fixedEnd + (int)atomicAdd(&a.queue[b], 1u);
         T.sync();
         int slot = s_item[team];
         while (slot < nslots) {
           int nxt = 0;
-          if (T.tw == 0 && lane == 0) nxt = (int)atomicAdd(&a.queue[b], 1u);
+          if (T.tw == 0 && lane == 0) nxt = fixedEnd + (int)atomicAdd(&a.queue[b], 1u);
           const unsigned better = wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
           if (better) atomicAdd(&s_better, 1u);
           if (T.tw == 0 && lane == 0) s_item[team] = nxt;
