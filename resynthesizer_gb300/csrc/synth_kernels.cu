@@ -1239,40 +1239,34 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
       const WaveTeam T{G, team, warp % G, team * G, lane, warp, p, s_key, s_n, s_np, s_fast, s_gather};
       const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
       const int visCur = a.pass == 0 ? b : 0x7ffffffe;
-      if (a.queue && !a.probeShare) {
-        // Three quarters of the batch in fixed shares -- the teams of a CTA
-        // take neighbouring slots, whose patches overlap in L1 -- then the
-        // rest handed out one slot at a time from the batch's queue, so that
-        // the batch ends when its last target does rather than when the team
-        // with the slowest share does.  (A team's next grab is in flight
-        // while it works.)
-        const int stride = gridDim.x * teamsPerBlock;
-        const int fixedEnd = (nslots * 3 / 4) / stride * stride;
-        for (int slot = blockIdx.x * teamsPerBlock + team; slot < fixedEnd; slot += stride) {
-          const unsigned better =
-              wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
-          if (better) atomicAdd(&s_better, 1u);
+      // Three quarters of the batch in fixed shares -- the teams of a CTA
+      // take neighbouring slots, whose patches overlap in L1 -- then the rest
+      // handed out one slot at a time from the batch's queue, so that the
+      // batch ends when its last target does rather than when the team with
+      // the slowest share does.  With probes shared by groups of 16 slots
+      // every slot stays in the fixed shares (a CTA's warps then read the
+      // same corpus windows).  One call site of wave_target: the kernel's
+      // code stays the size of one target's work.
+      const int stride = gridDim.x * teamsPerBlock;
+      const int fixedEnd = (a.queue && !a.probeShare) ? (nslots * 3 / 4) / stride * stride : nslots;
+      int slot = blockIdx.x * teamsPerBlock + team;
+      bool fixed = slot < fixedEnd;
+      if (!fixed && fixedEnd < nslots) {
+        if (T.tw == 0 && lane == 0) s_item[team] = fixedEnd + (int)atomicAdd(&a.queue[b], 1u);
+        T.sync();
+        slot = s_item[team];
+      }
+      while (slot < nslots) {
+        const unsigned better = wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
+        if (better) atomicAdd(&s_better, 1u);
+        if (fixed) {
+          slot += stride;
+          fixed = slot < fixedEnd;
+          if (fixed || fixedEnd >= nslots) continue;
         }
         if (T.tw == 0 && lane == 0) s_item[team] = fixedEnd + (int)atomicAdd(&a.queue[b], 1u);
         T.sync();
-        int slot = s_item[team];
-        while (slot < nslots) {
-          int nxt = 0;
-          if (T.tw == 0 && lane == 0) nxt = fixedEnd + (int)atomicAdd(&a.queue[b], 1u);
-          const unsigned better = wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
-          if (better) atomicAdd(&s_better, 1u);
-          if (T.tw == 0 && lane == 0) s_item[team] = nxt;
-          T.sync();
-          slot = s_item[team];
-        }
-      } else {
-        // Probes shared by groups of 16 slots: the warps of a CTA take 16
-        // consecutive slots together, so they read the same corpus windows.
-        for (int slot = blockIdx.x * teamsPerBlock + team; slot < nslots; slot += gridDim.x * teamsPerBlock) {
-          const unsigned better =
-              wave_target<NC, MAP>(a, pb, cv, ct, mt, b, visCur, b0, slot, sparse, T, terms, evals);
-          if (better) atomicAdd(&s_better, 1u);
-        }
+        slot = s_item[team];
       }
     }
     if (!a.inPlace) {
