@@ -252,6 +252,14 @@ int resynthPatchNeighbours(const unsigned char *hasValue, unsigned int width, un
                            unsigned int patchSize, const Coordinates *targets, unsigned int n, int useGrid,
                            Coordinates *offsets, unsigned int *counts);
 
+/* No counterpart in the reference.  Test entry of the device-side visit
+ * order of the directional and brushfire types (matchContextType 2..8): the
+ * n points (host memory, in the engine's row-major target order) reordered
+ * as lib/orderTarget.h:268-343 orders them -- the sort by the type's key from
+ * the bounding-box centre, then the banded shuffle drawn from the PRNG seeded
+ * with 1198472 -- computed by the kernels wavefront mode uses. */
+int resynthOrderTargets(int matchContextType, const Coordinates *points, unsigned int n, Coordinates *ordered);
+
 /* No counterpart in the reference.  Frozen-state best fit, as
  * resynthFrozenBestFit, for callers that cannot let a library allocate device
  * memory -- a host application that reserves the GPU's memory up front and

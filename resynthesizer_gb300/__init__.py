@@ -389,6 +389,18 @@ def image_synth_batch(items, opts: Options | None = None, concurrency: int = 8):
     return rc, [k[0] for k in keep], [reqs[i].result for i in range(len(items))], st.as_dict()
 
 
+def order_targets_device(match_context_type: int, points: np.ndarray) -> np.ndarray:
+    """resynthOrderTargets: the device-side visit order of a directional type."""
+    L = lib()
+    L.resynthOrderTargets.argtypes = [C.c_int, C.c_void_p, C.c_uint, C.c_void_p]
+    pts = np.ascontiguousarray(points, np.int32)
+    out = np.zeros_like(pts)
+    rc = L.resynthOrderTargets(match_context_type, _vp(pts), len(pts), _vp(out))
+    if rc:
+        raise RuntimeError(f"resynthOrderTargets rc={rc}: {last_error()}")
+    return out
+
+
 def grid_barrier_probe(rounds: int, absent_cta: int = -1, timeout_ns: int = 1_000_000_000):
     """resynthGridBarrierProbe: (barriers passed summed over CTAs, error bits)."""
     L = lib()

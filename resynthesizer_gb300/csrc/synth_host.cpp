@@ -251,6 +251,23 @@ int order_targets(int type, std::vector<Pt>& v, GlibcRand& rng) {
   return 0;
 }
 
+// The banded shuffle of lib/orderTarget.h:58-79 as a permutation of positions:
+// after it, position i holds what the sorted order had at perm[i].  It
+// depends only on the count and on the PRNG stream (which the directional
+// orders draw from for this shuffle alone), so the device can sort and the
+// host shuffle indices at the same time.
+std::vector<int> band_shuffle_perm(unsigned n) {
+  GlibcRand rng(1198472u);   // lib/engine.c:643
+  std::vector<int> idx(n);
+  for (unsigned i = 0; i < n; i++) idx[i] = (int)i;
+  const int last = (int)n - 1, half = (int)(n * 0.1);
+  for (int i = 0; i <= last; i++) {
+    const int lo = std::max(i - half, 0), hi = std::min(i + half, last);
+    std::swap(idx[i], idx[lo + (int)rng.range(0, (unsigned)(hi - lo))]);
+  }
+  return idx;
+}
+
 // ------------------------------------------------------------ the problem
 
 struct HostPrep {
@@ -751,6 +768,56 @@ void wait_stream(Stream& st, cudaEvent_t ev, int* cancel) {
   }
 }
 
+// The visit order of a directional or brushfire type (matchContextType 2..8,
+// lib/orderTarget.h:268-343) of the n row-major targets in dTargets, made on
+// the device into dOut; the banded shuffle's permutation is computed on the
+// host meanwhile.  Brushfire needs two short round trips: the rays of the few
+// targets next to a ray boundary come from the host's libm (as the
+// reference's do), and a NaN key -- the bounding-box centre is a target alone
+// on its ray -- sends the whole order to the host's qsort, whose treatment of
+// it no key sort reproduces.
+void order_directional(int type, const int2* dTargets, int n, int2* dOut, Arena& ar, Stream& st, cudaStream_t s,
+                       unsigned long long& h2d, unsigned long long& d2h, unsigned& launches) {
+  int* work = ar.alloc<int>(rs_order_ints(n));
+  const bool brush = type == 2 || type == 5 || type == 8;
+  int* dFlags = brush ? ar.alloc<int>(1 + 3 * (size_t)n) : nullptr;
+  CK(rs_order_begin(type, dTargets, n, work, dFlags, dFlags ? dFlags + 1 : nullptr, n, s));
+  launches += brush ? 3 : 2;
+  if (brush) CK(cudaMemcpyAsync(st.hostInts + 4, dFlags, sizeof(int), cudaMemcpyDeviceToHost, s));
+  const std::vector<int> perm = band_shuffle_perm((unsigned)n);   // host work while the device runs
+  if (brush) {
+    CK(cudaStreamSynchronize(s));
+    const int nflag = std::min(st.hostInts[4], n);
+    std::vector<int> flags(3 * (size_t)nflag), fix(2 * (size_t)nflag);
+    if (nflag) CK(cudaMemcpy(flags.data(), dFlags + 1, flags.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    d2h += 4 + flags.size() * sizeof(int);
+    for (int i = 0; i < nflag; i++) {
+      fix[2 * i] = flags[3 * i];
+      fix[2 * i + 1] = (int)ray_of(Pt{flags[3 * i + 1], flags[3 * i + 2]});
+    }
+    const int* dFix = nflag ? ar.upload(fix.data(), fix.size(), h2d) : nullptr;
+    CK(rs_order_rays(dTargets, n, work, dFix, nflag, s));
+    launches += nflag ? 3 : 2;
+    CK(cudaMemcpyAsync(st.hostInts + 5, rs_order_nan_flag(work, n), sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    d2h += 4;
+    if (st.hostInts[5]) {
+      std::vector<Pt> v((size_t)n);
+      CK(cudaMemcpy(v.data(), dTargets, (size_t)n * sizeof(int2), cudaMemcpyDeviceToHost));
+      d2h += (size_t)n * sizeof(int2);
+      GlibcRand rng(1198472u);
+      order_targets(type, v, rng);
+      CK(cudaMemcpyAsync(dOut, v.data(), (size_t)n * sizeof(int2), cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));   // v is pageable and about to go
+      h2d += (size_t)n * sizeof(int2);
+      return;
+    }
+  }
+  const int* dPerm = ar.upload(perm.data(), perm.size(), h2d);
+  CK(rs_order_finish(type, dTargets, n, work, dPerm, dOut, s));
+  launches += 14;
+}
+
 // The pass loop on device pixmaps.  dT is updated in place.  `prepared` is
 // the host preparation when the caller already made it (engine() on host maps).
 int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, uint8_t* dT, unsigned tw,
@@ -764,9 +831,9 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
   if (!cancel) cancel = &zero;
   const bool replay = opt.mode == RESYNTH_MODE_REPLAY;
   const bool randomOrder = p.matchContextType == 0 || p.matchContextType == 1;
-  // Wavefront runs with a random order prepare on the device; replay and the
-  // directional orders use the host preparation (the reference's exact order).
-  const bool devicePrep = !replay && randomOrder;
+  // Wavefront runs prepare on the device (the directional orders too, in the
+  // reference's exact order); replay uses the host preparation.
+  const bool devicePrep = !replay && p.matchContextType >= 0 && p.matchContextType <= 8;
   HostPrep local;
   if (!devicePrep && !prepared) {
     std::vector<uint8_t> tHost((size_t)tw * th * f.total_bpp), cHost((size_t)cw * ch * f.total_bpp);
@@ -832,6 +899,13 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     dp.pb.ncorpus = ncorpus;
     dp.pb.fullCorpus = (size_t)ncorpus == cn ? 1 : 0;
     pass_schedule(ntargets, ends, estimated);
+    if (!randomOrder) {
+      int2* ordered = ar.alloc<int2>(ntargets);
+      unsigned long long d2h = 0;
+      order_directional(p.matchContextType, dTargets, (int)ntargets, ordered, ar, st, s, h2d, d2h, launches);
+      stats.d2hBytes += d2h;
+      dTargets = ordered;
+    }
   } else {
     HostPrep& hp = *prepared;
     ntargets = (unsigned)hp.targets.size();
@@ -1597,7 +1671,7 @@ int run_engine_host(const TImageSynthParameters& p, const TFormatIndices& f, uin
   // All argument and data checks of the reference come before any device work
   // (lib/engine.c:591-646), in the reference's order.
   if (p.patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
-  const bool devicePrep = opt.mode != RESYNTH_MODE_REPLAY && (p.matchContextType == 0 || p.matchContextType == 1);
+  const bool devicePrep = opt.mode != RESYNTH_MODE_REPLAY && p.matchContextType >= 0 && p.matchContextType <= 8;
   HostPrep hp;
   if (devicePrep) {
     const size_t tn = (size_t)tw * th, cn = (size_t)cw * ch;
@@ -1664,9 +1738,10 @@ int image_synth_impl(ImageBuffer* img, ImageBuffer* mask, ImageBuffer* mask2, TI
   const unsigned d = bpp + 1;
   int zero0 = 0;
   if (!cancel) cancel = &zero0;
-  if (opt.mode != RESYNTH_MODE_REPLAY && (params->matchContextType == 0 || params->matchContextType == 1)) {
-    // Device path: the adaption runs on the GPU from one upload of the
-    // caller's buffers; only the reference's up-front checks use the host.
+  if (opt.mode != RESYNTH_MODE_REPLAY && params->matchContextType >= 0 && params->matchContextType <= 8) {
+    // Device path (wavefront mode, every visit order): the adaption runs on
+    // the GPU from one upload of the caller's buffers; only the reference's
+    // up-front checks use the host.
     if (params->patchSize > (unsigned)rs::kMaxNeighbors) return IMAGE_SYNTH_ERROR_PATCH_SIZE_EXCEEDED;
     ImageBuffer* cm = mask2 ? mask2 : mask;
     bool anyTarget = false, anyCorpus = false;
@@ -2118,6 +2193,26 @@ RS_EXPORT int resynthPatchNeighbours(const unsigned char* hasValue, unsigned int
         offsets[(size_t)t * (rs::kMaxNeighbors - 1) + i] = Coordinates{(int)(int16_t)(o & 0xffff), o >> 16};
       }
     }
+    return 0;
+  });
+}
+
+RS_EXPORT int resynthOrderTargets(int matchContextType, const Coordinates* points, unsigned int n,
+                                  Coordinates* ordered) {
+  if (!points || !ordered || !n) return fail(RESYNTH_ERROR_ARGUMENT, "resynthOrderTargets: bad argument");
+  if (matchContextType < 2 || matchContextType > 8)
+    return fail(RESYNTH_ERROR_ARGUMENT, "resynthOrderTargets: matchContextType must be 2..8");
+  return guarded("resynthOrderTargets", [&]() -> int {
+    Stream& st = thread_stream();
+    cudaStream_t s = st.s;
+    Arena ar(s);
+    unsigned long long h2d = 0, d2h = 0;
+    unsigned launches = 0;
+    const int2* dIn = ar.upload(reinterpret_cast<const int2*>(points), n, h2d);
+    int2* dOut = ar.alloc<int2>(n);
+    order_directional(matchContextType, dIn, (int)n, dOut, ar, st, s, h2d, d2h, launches);
+    CK(cudaMemcpyAsync(ordered, dOut, (size_t)n * sizeof(int2), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     return 0;
   });
 }

@@ -179,6 +179,20 @@ size_t rs_prep_batches_ints(int n, int nkeys);
 cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, size_t maskRow, const uint8_t* mask2,
                      size_t mask2Row, int w, int h, int bpp, uint8_t* target, uint8_t* corpus, cudaStream_t s);
 cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow, cudaStream_t s);
+// The directional and brushfire visit orders (matchContextType 2..8) on the
+// device, from the row-major target list: begin (bounding box; brushfire:
+// rays, listing as (index, dx, dy) the targets whose ray the host must
+// recompute), rays (brushfire: the host's rays for those as (index, ray)
+// pairs, the largest |q|^2 per ray, the NaN flag), finish (keys, stable radix
+// sort, banded-shuffle permutation `perm` from the host).  work:
+// rs_order_ints(n) ints.
+size_t rs_order_ints(int n);
+cudaError_t rs_order_begin(int type, const int2* targets, int n, int* work, int* flagCount, int* flags, int cap,
+                           cudaStream_t s);
+cudaError_t rs_order_rays(const int2* targets, int n, int* work, const int* fix, int nfix, cudaStream_t s);
+int* rs_order_nan_flag(int* work, int n);
+cudaError_t rs_order_finish(int type, const int2* targets, int n, int* work, const int* perm, int2* out,
+                            cudaStream_t s);
 cudaError_t rs_vis_init(const uint8_t* has, int npx, int* vis, cudaStream_t s);
 cudaError_t rs_vis_to_has(const int* vis, int npx, uint8_t* has, cudaStream_t s);
 cudaError_t rs_cell_min(const int* vis, int tw, int th, int* cellMin, cudaStream_t s);

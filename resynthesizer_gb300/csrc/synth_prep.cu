@@ -7,6 +7,7 @@
 // bucketed by (band, colour phase) with a counting sort so that batch b is
 // targets[batchStart[b] .. batchStart[b+1]).
 #include <algorithm>
+#include <climits>
 #include <cstdint>
 
 #include "synth_internal.h"
@@ -424,5 +425,256 @@ extern "C" cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t
 extern "C" cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow,
                                   cudaStream_t s) {
   k_unadapt<<<std::min(blocks_for(w * h, 256), 4096), 256, 0, s>>>(target, w, h, bpp, img, imgRow);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Directional and brushfire visit orders on the device (lib/orderTarget.h:
+// 154-343, lib/brushfire.h:62-163).  The reference sorts the target points
+// with libc qsort (glibc: a merge sort) and comparators that never return 0:
+// the "more" comparators keep equal keys in input order, the "less" ones
+// reverse them.  Both are a stable sort of 32-bit keys -- over the input
+// reversed for the "less" comparators -- done here as an LSD radix sort of
+// four 8-bit digits.  Keys: |dx| or |dy| from the bounding-box centre for the
+// directional types (ordering by dx^2 is ordering by |dx|); for brushfire,
+// the float |p|^2 / (largest |q|^2 on p's ray), whose bit pattern orders like
+// the value for the non-negative floats it takes.  The banded shuffle that
+// follows the sort (lib/orderTarget.h:58-79) is a fixed permutation of
+// positions given by the host.
+namespace rs {
+namespace {
+
+constexpr int kOrderChunk = 8192;
+constexpr int kRays = 401;
+
+// work layout (ints): [0..4) bounding box (minx, miny, maxx, maxy),
+// [4] NaN flag, [8 .. 8 + kRays) largest |q|^2 per ray, then n rays, keys A,
+// keys B, values A, values B, and the digit counts and their offsets.
+struct OrderWork {
+  int* box;
+  int* nan;
+  unsigned* maxr;
+  int* rays;
+  unsigned *keysA, *keysB;
+  int *valsA, *valsB;
+  int *counts, *offsets;
+  int nchunks;
+  __host__ __device__ OrderWork(int* w, int n) {
+    nchunks = n > 0 ? (n + kOrderChunk - 1) / kOrderChunk : 1;
+    box = w;
+    nan = w + 4;
+    maxr = reinterpret_cast<unsigned*>(w + 8);
+    rays = w + 8 + kRays;
+    keysA = reinterpret_cast<unsigned*>(rays + n);
+    keysB = keysA + n;
+    valsA = reinterpret_cast<int*>(keysB + n);
+    valsB = valsA + n;
+    counts = valsB + n;
+    offsets = counts + 256 * nchunks;
+  }
+  static size_t ints(int n) {
+    const size_t nchunks = n > 0 ? ((size_t)n + kOrderChunk - 1) / kOrderChunk : 1;
+    return 8 + kRays + 5 * (size_t)n + 2 * 256 * nchunks + 1;
+  }
+};
+
+__global__ void k_order_init(int* w, int n) {
+  OrderWork W(w, n);
+  for (int i = threadIdx.x; i < kRays; i += blockDim.x) W.maxr[i] = 0;
+  if (threadIdx.x == 0) {
+    W.box[0] = W.box[1] = INT_MAX;   // lib/engineTypes.h:187-226 starts from these
+    W.box[2] = W.box[3] = 0;
+    *W.nan = 0;
+  }
+}
+
+__global__ void k_order_bbox(const int2* t, int n, int* w) {
+  OrderWork W(w, n);
+  int x0 = INT_MAX, y0 = INT_MAX, x1 = 0, y1 = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 p = t[i];
+    x0 = min(x0, p.x);
+    y0 = min(y0, p.y);
+    x1 = max(x1, p.x);
+    y1 = max(y1, p.y);
+  }
+  x0 = __reduce_min_sync(0xffffffffu, x0);
+  y0 = __reduce_min_sync(0xffffffffu, y0);
+  x1 = __reduce_max_sync(0xffffffffu, x1);
+  y1 = __reduce_max_sync(0xffffffffu, y1);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&W.box[0], x0);
+    atomicMin(&W.box[1], y0);
+    atomicMax(&W.box[2], x1);
+    atomicMax(&W.box[3], y1);
+  }
+}
+
+__device__ __forceinline__ int2 rel(const OrderWork& W, int2 p) {
+  const int cx = (W.box[2] - W.box[0]) / 2 + W.box[0], cy = (W.box[3] - W.box[1]) / 2 + W.box[1];
+  return make_int2(p.x - cx, p.y - cy);
+}
+
+// Brushfire rays: (unsigned)(atan2(y, x) * 200 / pi + 200) in double, as the
+// reference computes it.  The device atan2 may differ from the host libm's
+// in the last bits, which can only matter where the value lies next to a
+// whole number (the axes and diagonals): those targets are listed for the
+// host to recompute, as (index, dx, dy).
+__global__ void k_order_rays(const int2* t, int n, int* w, int* flagCount, int* flags, int cap) {
+  OrderWork W(w, n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 p = rel(W, t[i]);
+    const double v = atan2((double)(float)p.y, (double)(float)p.x) * 200 / 3.1415926535897932384626433832795 + 200;
+    W.rays[i] = (int)(unsigned)v;
+    if (fabs(v - rint(v)) < 1e-9) {
+      const int k = atomicAdd(flagCount, 1);
+      if (k < cap) {
+        flags[3 * k] = i;
+        flags[3 * k + 1] = p.x;
+        flags[3 * k + 2] = p.y;
+      }
+    }
+  }
+}
+
+__global__ void k_order_fix_rays(const int* fix, int nfix, int* w, int n) {
+  OrderWork W(w, n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nfix; i += gridDim.x * blockDim.x)
+    W.rays[fix[2 * i]] = fix[2 * i + 1];
+}
+
+__global__ void k_order_maxr(const int2* t, int n, int* w) {
+  OrderWork W(w, n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 p = rel(W, t[i]);
+    atomicMax(&W.maxr[W.rays[i]], (unsigned)(p.x * p.x + p.y * p.y));
+  }
+}
+
+// 0 / 0: the centre is a target and alone on its ray.  The comparators then
+// meet a NaN, which orders like no key; the host makes that order.
+__global__ void k_order_nan(const int2* t, int n, int* w) {
+  OrderWork W(w, n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int2 p = rel(W, t[i]);
+    if (p.x == 0 && p.y == 0 && W.maxr[W.rays[i]] == 0) *W.nan = 1;
+  }
+}
+
+__global__ void k_order_keys(int type, const int2* t, int n, int* w) {
+  OrderWork W(w, n);
+  const bool reverse = type == 5 || type == 6 || type == 7;   // the "less" comparators
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int src = reverse ? n - 1 - i : i;
+    const int2 p = rel(W, t[src]);
+    unsigned key;
+    if (type == 3 || type == 6 || type == 4 || type == 7) {
+      const unsigned a = (unsigned)abs(type == 3 || type == 6 ? p.x : p.y);
+      key = type == 3 || type == 4 ? ~a : a;   // 3, 4: descending; 6, 7: ascending
+    } else {
+      const float prop = __fdiv_rn((float)(p.y * p.y + p.x * p.x), __uint2float_rn(W.maxr[W.rays[src]]));
+      const unsigned b = __float_as_uint(prop);
+      key = type == 5 ? b : ~b;                 // 2, 8: descending; 5: ascending
+    }
+    W.keysA[i] = key;
+    W.valsA[i] = src;
+  }
+}
+
+// One 8-bit digit pass of the radix sort: per chunk, the count of each digit
+// value, stored digit-major ([digit][chunk]) for one exclusive scan.
+__global__ void k_order_hist(const unsigned* keys, int n, int shift, int* counts, int nchunks) {
+  __shared__ int hist[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < kOrderChunk; i += blockDim.x) {
+    const int j = blockIdx.x * kOrderChunk + i;
+    if (j >= n) break;
+    atomicAdd(&hist[(keys[j] >> shift) & 0xFFu], 1);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) counts[(size_t)i * nchunks + blockIdx.x] = hist[i];
+}
+
+// Stable scatter of one digit pass (as k_scatter: warps of a chunk in order,
+// lanes of a warp by rank among same-digit lanes).
+__global__ void k_order_scatter(const unsigned* keys, const int* vals, int n, int shift, const int* offsets,
+                                int nchunks, unsigned* keysOut, int* valsOut) {
+  __shared__ int cnt[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) cnt[i] = 0;
+  __syncthreads();
+  const int chunk = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  for (int base = 0; base < kOrderChunk; base += blockDim.x) {
+    const int j = chunk * kOrderChunk + base + threadIdx.x;
+    const int d = j < n ? (int)((keys[j] >> shift) & 0xFFu) : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    int before = 0;
+    for (int w = 0; w < nwarps; w++) {
+      if (warp == w) {
+        if (d >= 0) before = cnt[d];
+        __syncwarp();
+        if (lane == leader && d >= 0) cnt[d] = before + __popc(peers);
+      }
+      __syncthreads();
+    }
+    if (d >= 0) {
+      const int pos = offsets[(size_t)d * nchunks + chunk] + before + __popc(peers & lt);
+      keysOut[pos] = keys[j];
+      valsOut[pos] = vals[j];
+    }
+  }
+}
+
+// out[i] = the target at sorted position perm[i] (the banded shuffle).
+__global__ void k_order_gather(const int2* t, const int* sorted, const int* perm, int n, int2* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = t[sorted[perm[i]]];
+}
+
+int grid_of(int n) { return std::max(1, std::min(blocks_for(n, 256), 2048)); }
+
+}  // namespace
+}  // namespace rs
+
+extern "C" size_t rs_order_ints(int n) { return OrderWork::ints(n); }
+
+extern "C" cudaError_t rs_order_begin(int type, const int2* targets, int n, int* work, int* flagCount, int* flags,
+                                      int cap, cudaStream_t s) {
+  k_order_init<<<1, 512, 0, s>>>(work, n);
+  k_order_bbox<<<grid_of(n), 256, 0, s>>>(targets, n, work);
+  if (type == 2 || type == 5 || type == 8) {
+    cudaMemsetAsync(flagCount, 0, sizeof(int), s);
+    k_order_rays<<<grid_of(n), 256, 0, s>>>(targets, n, work, flagCount, flags, cap);
+  }
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_order_rays(const int2* targets, int n, int* work, const int* fix, int nfix,
+                                     cudaStream_t s) {
+  if (nfix) k_order_fix_rays<<<grid_of(nfix), 256, 0, s>>>(fix, nfix, work, n);
+  k_order_maxr<<<grid_of(n), 256, 0, s>>>(targets, n, work);
+  k_order_nan<<<grid_of(n), 256, 0, s>>>(targets, n, work);
+  return cudaGetLastError();
+}
+
+extern "C" int* rs_order_nan_flag(int* work, int n) { return OrderWork(work, n).nan; }
+
+extern "C" cudaError_t rs_order_finish(int type, const int2* targets, int n, int* work, const int* perm, int2* out,
+                                       cudaStream_t s) {
+  OrderWork W(work, n);
+  k_order_keys<<<grid_of(n), 256, 0, s>>>(type, targets, n, work);
+  unsigned *ka = W.keysA, *kb = W.keysB;
+  int *va = W.valsA, *vb = W.valsB;
+  for (int shift = 0; shift < 32; shift += 8) {
+    k_order_hist<<<W.nchunks, 256, 0, s>>>(ka, n, shift, W.counts, W.nchunks);
+    k_scan_wide<<<1, 1024, 0, s>>>(W.counts, 256 * W.nchunks, W.offsets);
+    k_order_scatter<<<W.nchunks, 256, 0, s>>>(ka, va, n, shift, W.offsets, W.nchunks, kb, vb);
+    std::swap(ka, kb);
+    std::swap(va, vb);
+  }
+  k_order_gather<<<grid_of(n), 256, 0, s>>>(targets, va, perm, n, out);
   return cudaGetLastError();
 }
