@@ -53,10 +53,10 @@ constexpr int kCell = 1 << kCellShift;
 // Grid-wide barrier of the persistent wavefront kernel (cooperative launch):
 // zeroed by the host before every launch.
 struct GridBar {
-  unsigned int count;            // CTAs arrived in the current generation
-  unsigned int gen;              // generation, advanced by the last CTA to arrive
-  unsigned int stop;             // written by that CTA: nonzero = every CTA leaves
+  unsigned int count;            // arrivals so far (barrier k is passed once it reaches k * CTAs)
+  unsigned int stopInv;          // 0, or ~k: every CTA leaves at barrier k (the earliest requested)
   unsigned int error;            // error bits of a launch that has no Counters of its own (many requests)
+  unsigned int pad;
 };
 
 // Most requests one persistent many-request launch takes (its slot prefix

@@ -1088,11 +1088,6 @@ __global__ void __launch_bounds__(512, 2) k_wave(WaveArgs a) {
 
 // ------------------------------------------------ persistent wavefront pass
 
-__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
 // A poll that neither caches the line in L1 nor invalidates L1 (an acquire
 // load would, on every poll, taking the L1 away from a working CTA on the
 // same SM); the acquire fence comes once, after the value changed.
@@ -1102,56 +1097,54 @@ __device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
   return v;
 }
 __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
-__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
 
-// Barrier across every CTA of a cooperative launch.  Thread 0 of each CTA
-// publishes the CTA's writes (fence), arrives, and waits for the generation
-// to advance; the last CTA to arrive decides for everyone whether the run
-// stops here (the host's abort flag, or an error any CTA reported before
-// arriving) and releases the others.  A wait gives up after timeoutNs of
-// global time: the CTA records kErrBarrier and leaves, so a CTA that never
-// arrives makes every other CTA leave at its next barrier instead of
-// spinning forever.  Returns true when the CTA must leave.
-__device__ bool grid_barrier(GridBar* gb, const volatile int* abortFlag, unsigned* err, long long timeoutNs) {
+// Barrier across every CTA of a cooperative launch, on a counter that only
+// grows: thread 0 of each CTA publishes the CTA's writes (fence), adds its
+// arrival without waiting for the result, and polls until the count reaches
+// k * CTAs for the CTA's k-th barrier -- no CTA has to act for the others, so
+// the release is one L2 round trip after the last arrival.  A CTA that must
+// stop the run (the host's cancel flag, a failed copy) asks, between two
+// barriers, for everyone to leave at the next one (request_stop): all CTAs
+// then leave at the same barrier.  A wait gives up after timeoutNs of global
+// time: the CTA records kErrBarrier and leaves, so a CTA that never arrives
+// makes every other CTA leave at its next barrier instead of spinning
+// forever.  nbar counts the CTA's barriers.  Returns true when the CTA must
+// leave.
+__device__ __forceinline__ void request_stop(GridBar* gb, unsigned nbar) {
+  atomicMax(&gb->stopInv, ~(nbar + 1u));
+}
+
+__device__ bool grid_barrier(GridBar* gb, unsigned& nbar, unsigned* err, long long timeoutNs) {
   __shared__ unsigned s_stop;
   __syncthreads();
+  const unsigned k = ++nbar;
   if (threadIdx.x == 0) {
-    const unsigned gen = ld_acquire_gpu(&gb->gen);
     __threadfence();
-    const unsigned arrived = atomicAdd(&gb->count, 1u);
-    unsigned stop = 0;
-    if (arrived == gridDim.x - 1) {
-      __threadfence();
-      stop = (*abortFlag != 0 || *(volatile unsigned*)err != 0u) ? 1u : 0u;
-      atomicExch(&gb->count, 0u);
-      *(volatile unsigned*)&gb->stop = stop;
-      st_release_gpu(&gb->gen, gen + 1u);
+    atomicAdd(&gb->count, 1u);
+    const unsigned target = k * gridDim.x;
+    const unsigned long long t0 = global_ns();
+    bool late = false;
+    unsigned nap = 32;
+    while ((int)(ld_relaxed_gpu(&gb->count) - target) < 0) {
+      if ((long long)(global_ns() - t0) > timeoutNs) {
+        late = true;
+        break;
+      }
+      __nanosleep(nap);
+      if (nap < 256) nap <<= 1;
+    }
+    fence_acq_rel_gpu();
+    unsigned stop = 1u;
+    if (late) {
+      atomicOr(err, kErrBarrier);
     } else {
-      const unsigned long long t0 = global_ns();
-      bool late = false;
-      unsigned nap = 32;
-      while (ld_relaxed_gpu(&gb->gen) == gen) {
-        if ((long long)(global_ns() - t0) > timeoutNs) {
-          late = true;
-          break;
-        }
-        __nanosleep(nap);
-        if (nap < 256) nap <<= 1;
-      }
-      fence_acq_rel_gpu();
-      if (late) {
-        atomicOr(err, kErrBarrier);
-        stop = 1u;
-      } else {
-        stop = *(volatile unsigned*)&gb->stop;
-      }
+      const unsigned inv = *(volatile unsigned*)&gb->stopInv;
+      stop = (inv != 0u && ~inv <= k) ? 1u : 0u;
     }
     s_stop = stop;
   }
@@ -1213,9 +1206,12 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
       ok = stage_words(scpx, pb.cpxPad, cwords, bar);
       cv.px = scpx;
     }
-    // A CTA whose copy failed does no work but still meets every barrier; the
-    // barrier's leader sees the error and stops the run for all.
-    if (!ok && threadIdx.x == 0) atomicOr(&a.ctr->error, kErrStage);
+    // A CTA whose copy failed does no work but still meets the first barrier,
+    // where every CTA leaves.
+    if (!ok && threadIdx.x == 0) {
+      atomicOr(&a.ctr->error, kErrStage);
+      request_stop(a.gbar, 0);
+    }
   }
   load_half_tables(pb, ct, mt);
   __shared__ unsigned long long s_key[16];
@@ -1225,13 +1221,16 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
   const int wpb = blockDim.x >> 5;
   if (threadIdx.x == 0) s_better = 0;
   __syncthreads();
-  unsigned terms = 0, evals = 0, committed = 0;
+  unsigned terms = 0, evals = 0, committed = 0, nbar = 0;
   for (int b = a.batch; b < a.batchEnd; b++) {
     const int b0 = a.batchStart[b];
     const int nslots = a.batchStart[b + 1] - b0;
     // An empty batch changes nothing: every CTA reads the same boundaries, so
     // all of them skip its barriers together.
     if (nslots == 0) continue;
+    // The host's cancel flag (host memory, slow to read) is read by one
+    // thread while the batch runs; it stops the run at the batch's end.
+    if (blockIdx.x == 0 && threadIdx.x == 0 && *a.abortFlag) request_stop(a.gbar, nbar);
     if (ok) {
       const int G = team_size(nslots);
       const int teamsPerBlock = wpb / G;
@@ -1270,10 +1269,10 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
       }
     }
     if (!a.inPlace) {
-      if (grid_barrier(a.gbar, a.abortFlag, &a.ctr->error, a.barTimeoutNs)) break;
+      if (grid_barrier(a.gbar, nbar, &a.ctr->error, a.barTimeoutNs)) break;
       committed += commit_batch(a, b);
     }
-    if (grid_barrier(a.gbar, a.abortFlag, &a.ctr->error, a.barTimeoutNs)) break;
+    if (grid_barrier(a.gbar, nbar, &a.ctr->error, a.barTimeoutNs)) break;
   }
   for (int o = 16; o > 0; o >>= 1) committed += __shfl_xor_sync(kFull, committed, o);
   if (lane == 0 && committed) atomicAdd(&s_better, committed);
@@ -1289,11 +1288,12 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
 // Test kernel of the grid barrier: every CTA but CTA `absent` meets `rounds`
 // barriers; CTA `absent` (when in range) leaves at once, so the others' waits
 // must run out.
-__global__ void k_barrier_probe(GridBar* gb, const volatile int* abortFlag, unsigned* err, int rounds, int absent,
-                                long long timeoutNs, unsigned* passed) {
+__global__ void k_barrier_probe(GridBar* gb, unsigned* err, int rounds, int absent, long long timeoutNs,
+                                unsigned* passed) {
   if ((int)blockIdx.x == absent) return;
+  unsigned nbar = 0;
   for (int r = 0; r < rounds; r++) {
-    if (grid_barrier(gb, abortFlag, err, timeoutNs)) return;
+    if (grid_barrier(gb, nbar, err, timeoutNs)) return;
     if (threadIdx.x == 0) atomicAdd(passed, 1u);
   }
 }
@@ -1372,10 +1372,12 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi_persistent(const WaveArgs
   __shared__ unsigned long long s_key[16];
   __shared__ int s_n[16], s_np[16], s_fast[16], s_gather[16], s_item[16];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned nbar = 0;
   for (int b = 0; b < steps; b++) {
     const int* pre = prefix + (size_t)b * (nreq + 1);
     const int total = pre[nreq];
     if (total == 0) continue;   // the same for every CTA: no barrier needed
+    if (blockIdx.x == 0 && threadIdx.x == 0 && *abortFlag) request_stop(gb, nbar);
     for (int r = threadIdx.x; r <= nreq; r += blockDim.x) sPrefix[r] = pre[r];
     __syncthreads();
     const int G = team_size(total);
@@ -1409,7 +1411,7 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi_persistent(const WaveArgs
       gs = s_item[team];
     }
     if (staged) {
-      if (grid_barrier(gb, abortFlag, err, timeoutNs)) return;
+      if (grid_barrier(gb, nbar, err, timeoutNs)) return;
       for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         const int r = multi_request(sPrefix, nreq, g);
         const WaveArgs& a = jobs[r];
@@ -1427,7 +1429,7 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi_persistent(const WaveArgs
         }
       }
     }
-    if (grid_barrier(gb, abortFlag, err, timeoutNs)) return;
+    if (grid_barrier(gb, nbar, err, timeoutNs)) return;
   }
 }
 
@@ -1844,8 +1846,7 @@ extern "C" __attribute__((visibility("default"))) int resynthGridBarrierProbe(in
   if (!rs_persistent_supported()) return rs_fail(RESYNTH_ERROR_DEVICE, "cooperative launches not supported");
   struct Dev {
     GridBar gb;
-    int abortFlag;
-    unsigned err, passed, pad;
+    unsigned err, passed;
   };
   Dev* d = nullptr;
   cudaError_t e = cudaMalloc(&d, sizeof(Dev));
@@ -1853,10 +1854,9 @@ extern "C" __attribute__((visibility("default"))) int resynthGridBarrierProbe(in
   const int grid = sm_count() * 2;
   if (e == cudaSuccess) {
     GridBar* gb = &d->gb;
-    const volatile int* ab = &d->abortFlag;
     unsigned* err = &d->err;
     unsigned* pass = &d->passed;
-    void* params[] = {&gb, (void*)&ab, &err, &rounds, &absentCta, &timeoutNs, &pass};
+    void* params[] = {&gb, &err, &rounds, &absentCta, &timeoutNs, &pass};
     e = cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(grid), dim3(256), params, 0, nullptr);
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
