@@ -14,7 +14,8 @@
  *     order), stopping when betters < n/10 after at least minPasses
  *     (lib/refiner.h:42-122, lib/passes.h:67-93);
  *   - a pass is a sequence of batches: pass 0 cuts the ranks into bands of
- *     16, 32, 64, ... targets (random orders) or of equal widths of at least
+ *     f, 2f, 4f, ... targets with f = 16, or n / 1024 when larger for a
+ *     problem with context (random orders), or of equal widths of at least
  *     1024 (directional), later passes use one band, and every band is split
  *     into k x k colour phases by (x mod k, y mod k);
  *   - within a batch, targets see the state left by earlier batches only
@@ -421,7 +422,10 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
       if (pass == 0) {
         /* random orders: 16, 32, 64, ...; directional: equal widths of at
          * least 1024 */
-        const double first = opt->firstBatch ? opt->firstBatch : (randomOrder ? 16.0 : 1024.0);
+        /* random orders: 16, or n / 1024 when larger for problems with
+         * context (wave_first_band in synth_host.cpp) */
+        const unsigned firstRandom = context && (unsigned)n / 1024u > 16u ? (unsigned)n / 1024u : 16u;
+        const double first = opt->firstBatch ? opt->firstBatch : (randomOrder ? (double)firstRandom : 1024.0);
         const double growth = (opt->bandGrowth ? opt->bandGrowth : 200u) / 100.0;
         double size = randomOrder ? first : fmax(first, ceil((double)end / WO_MAX_BANDS)), b = 0;
         while (b < end && nb < WO_MAX_BANDS - 1) {

@@ -60,7 +60,7 @@ def frozen():
 # on a GB300 give these same outputs.
 WAVE_FULL = {
     "render1024": ("710baea67bc0c8500ffee84cb1251b01baeb669d22987efcde6304f5d6489edd", 3, [1048576, 51668, 23402]),
-    "heal4096": ("1910cd1e91e8b08d462a8a5f74a1ce76df5f85f509466f2282a1bc33d7989b53", 2, [1523352, 59065]),
+    "heal4096": ("6339cdc79ad835d4363eb096c3facba71d2cc81fc663fc10540c6c1cd4146d65", 2, [1523352, 59388]),
     "mapstyle2048": ("45f09923a9f0f492c256d8752cf9eecb04ee2ff39533f0a7cd86c43d4a104091", 2, [4194304, 71126]),
 }
 

@@ -1,6 +1,7 @@
 """The wavefront oracle (oracle/wave_oracle.c): a plain-C restatement of the
 library's default mode -- random visit order by a pixel hash, bands of
-16, 32, 64 ... targets cut into k x k colour phases, visit stamps, patches
+f, 2f, 4f ... targets (f = 16, or n / 1024 for heals) cut into k x k colour
+phases, visit stamps, patches
 from the sorted offsets within min(box diagonal, 256), deduplicated
 continuations then counter-hashed probes, the first strict minimum of the
 patch metric, staged stores, the reference's stop rule.  Its outputs on the
