@@ -747,7 +747,7 @@ def main():
     dev = torch.device("cuda", local)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > 129 MB L2
     stream = torch.cuda.current_stream()
-    opts = R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=args.warps, batchLaunches=int(args.batch_launches))
+    opts = R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=args.warps, batchLaunches=1 if args.batch_launches else 0)
 
     if args.profile_once:
         ms, stats = device_timing(R, torch, wl, opts, 1, 1, flush, stream)
@@ -775,7 +775,8 @@ def main():
     # events on the library's stream, against the two on-chip peaks that
     # bound it (measured here) and, as a secondary figure, the HBM copy peak
     _, pst = device_timing(R, torch, wl, R.options(mode=R.MODE_WAVEFRONT, profile=1, warpsPerBlock=args.warps,
-                                                   batchLaunches=int(args.batch_launches)), 1, 0, flush, stream)
+                                                   batchLaunches=1 if args.batch_launches else 0), 1, 0, flush,
+                                  stream)
     prof = pst[0]
     wave_ms_per_launch = prof["waveMs"] / max(1, prof["waveLaunches"])
     terms_per_launch = prof["waveTerms"] / max(1, prof["waveLaunches"])
@@ -790,7 +791,10 @@ def main():
     bound = max(fr, key=fr.get)
     roof = {"bound": bound, "achieved": smem_gbs if bound == "smem" else int_gops,
             "peak": smem_peak if bound == "smem" else int_peak, "unit": "GB/s" if bound == "smem" else "G int ops/s",
-            "frac": fr[bound], "traffic": WAVE_DRAM_BYTES.get(wname), "kernel": "k_wave_persistent",
+            "frac": fr[bound], "traffic": WAVE_DRAM_BYTES.get(wname),
+            "kernel": "k_wave" if prof.get("launchMode") == 2 else "k_wave_persistent",
+            "launch_mode": {0: "persistent, 16 warps per CTA", 1: "persistent, 8 warps per CTA",
+                            2: "one launch per batch", 3: "persistent"}.get(prof.get("launchMode")),
             "peak_source": "measured in this run: resynthMicrobench (conflict-free 16-byte shared loads; chains of "
                            "32-bit add and xor), best of five CUDA-event-timed launches",
             "smem": {"achieved": smem_gbs, "peak": smem_peak, "unit": "GB/s", "frac": fr["smem"],
@@ -816,7 +820,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": WORKLOAD if wname == "render1024" else wname, "target": f"{tw}x{th}",
                    "corpus": f"{cw}x{ch}", "target_px": target_px, "mode": "wavefront",
-                   "launch": "one launch per batch" if args.batch_launches else "one persistent launch per pass",
+                   "launch": "one launch per batch" if args.batch_launches else
+                             "tuned per problem class: persistent launches per pass or one launch per batch",
                    "l2": "flushed (256 MB write) between steps, outside the timed intervals",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "evals_per_s": evals_per_s,

@@ -162,8 +162,10 @@ typedef struct {
   int graphs;                 /* wavefront: launch each pass as one captured CUDA graph */
   int separateRequests;       /* imageSynthBatch: one stream per request instead of the many-request launches */
   unsigned int bandGrowthLarge; /* wavefront: growth in percent of pass-0 bands of at least 1/64 of the pass (0 = default) */
-  int batchLaunches;          /* wavefront: one kernel launch per batch instead of one persistent (cooperative)
-                                 launch per pass with grid barriers between batches; the output is the same */
+  int batchLaunches;          /* wavefront: how passes are launched (the output is the same): 0 = chosen per
+                                 problem class across calls (persistent cooperative launches with grid barriers
+                                 between batches, 16 or 8 warps per CTA, or one launch per batch: the fastest of
+                                 the first three calls of the class); 1 = one launch per batch; 2 = persistent */
 } TResynthOptions;
 
 typedef struct {
@@ -180,6 +182,8 @@ typedef struct {
   double waveMs;                  /* profile: summed duration of the per-target synthesis kernels */
   unsigned int waveLaunches;      /* profile: how many launches waveMs covers */
   unsigned long long waveTerms;   /* profile: neighbour terms those launches evaluated */
+  int launchMode;                 /* wavefront passes ran as: 0 persistent (16 warps per CTA), 1 persistent (8),
+                                     2 one launch per batch, 3 persistent (the caller's warps); -1 replay */
 } TResynthStats;
 
 /* Default options (wavefront mode, or the mode named by the environment

@@ -78,14 +78,14 @@ class Stats(C.Structure):
                 ("passes", C.c_uint), ("passLength", C.c_uint * 6), ("betters", C.c_uint * 6),
                 ("launches", C.c_uint), ("deviceMs", C.c_double), ("totalMs", C.c_double),
                 ("h2dBytes", C.c_ulonglong), ("d2hBytes", C.c_ulonglong), ("waveMs", C.c_double),
-                ("waveLaunches", C.c_uint), ("waveTerms", C.c_ulonglong)]
+                ("waveLaunches", C.c_uint), ("waveTerms", C.c_ulonglong), ("launchMode", C.c_int)]
 
     def as_dict(self) -> dict:
         return dict(visits=self.visits, evals=self.evals, terms=self.terms, passes=self.passes,
                     passLength=list(self.passLength)[: self.passes], betters=list(self.betters)[: self.passes],
                     launches=self.launches, deviceMs=self.deviceMs, totalMs=self.totalMs,
                     h2dBytes=self.h2dBytes, d2hBytes=self.d2hBytes, waveMs=self.waveMs,
-                    waveLaunches=self.waveLaunches, waveTerms=self.waveTerms)
+                    waveLaunches=self.waveLaunches, waveTerms=self.waveTerms, launchMode=self.launchMode)
 
 
 PROGRESS = C.CFUNCTYPE(None, C.c_int, C.c_void_p)

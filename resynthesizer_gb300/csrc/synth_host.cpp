@@ -695,37 +695,39 @@ void set_tuned_warps(uint64_t key, int warps) {
   g_tunedWarps[key] = warps;
 }
 
-// Warps per CTA of the persistent pass, tuned across calls per problem class:
-// the first call of a class runs with 16 warps, the second with 8, each timing
-// its first refinement pass; later calls use the faster (8 only if at least
-// 3 % faster).  Fewer warps per CTA mean more CTAs meeting at every grid
-// barrier, so the per-batch tuning's answer does not apply here.  The output
-// does not depend on the choice.
-struct PersistentTune {
-  int trials = 0, best = 0;
-  float ms[2] = {0, 0};
+// How a problem class's passes are launched, tuned across calls: the first
+// three calls of a class (colour and map channels, patch size, corpus and
+// target sizes) run the persistent pass with 16 warps per CTA, with 8, and
+// one launch per batch; each records the synthesis's device time, and later
+// calls use the fastest.  The persistent pass saves a launch per batch but
+// pays a grid barrier per batch, and with fewer warps per CTA more CTAs meet
+// at each barrier, so which wins depends on the problem (texture synthesis
+// with many small batches gains most from it).  The output does not depend on
+// the choice.
+enum LaunchConfig { kPersistent16 = 0, kPersistent8 = 1, kPerBatch = 2, kLaunchConfigs = 3 };
+struct LaunchTune {
+  int trials = 0, best = -1;
+  double ms[kLaunchConfigs] = {0, 0, 0};
 };
-std::map<uint64_t, PersistentTune> g_persistentTune;
+std::map<uint64_t, LaunchTune> g_launchTune;
 
-int persistent_warps(uint64_t key, int& trial) {
-  static const int kTry[2] = {16, 8};
+int launch_config(uint64_t key, bool& trial) {
   std::lock_guard<std::mutex> lock(g_tuneMu);
-  PersistentTune& t = g_persistentTune[key];
-  if (t.best) {
-    trial = -1;
-    return t.best;
-  }
-  trial = t.trials;
-  return kTry[trial];
+  LaunchTune& t = g_launchTune[key];
+  trial = t.best < 0;
+  return trial ? t.trials : t.best;
 }
 
-void persistent_result(uint64_t key, int trial, float ms) {
+void launch_result(uint64_t key, int config, double ms) {
   std::lock_guard<std::mutex> lock(g_tuneMu);
-  PersistentTune& t = g_persistentTune[key];
-  if (t.best || trial != t.trials) return;   // another call of the class got there first
-  t.ms[trial] = ms;
-  t.trials++;
-  if (t.trials == 2) t.best = t.ms[1] < 0.97f * t.ms[0] ? 8 : 16;
+  LaunchTune& t = g_launchTune[key];
+  if (t.best >= 0 || config != t.trials) return;   // another call of the class got there first
+  t.ms[config] = ms;
+  if (++t.trials == kLaunchConfigs) {
+    t.best = 0;
+    for (int c = 1; c < kLaunchConfigs; c++)
+      if (t.ms[c] < t.ms[t.best]) t.best = c;
+  }
 }
 
 // Radius (squared) of the offset list used by the wavefront mode: enough for
@@ -841,6 +843,9 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
   int zero = 0;
   if (!cancel) cancel = &zero;
   const bool replay = opt.mode == RESYNTH_MODE_REPLAY;
+  int launchCfg = -100;      // >= 0: this call tries that launch configuration (launch_config)
+  uint64_t launchKey = 0;
+  stats.launchMode = -1;
   const bool randomOrder = p.matchContextType == 0 || p.matchContextType == 1;
   // Wavefront runs prepare on the device (the directional orders too, in the
   // reference's exact order); replay uses the host preparation.
@@ -1041,15 +1046,23 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     const uint64_t tuneKey = (uint64_t)dp.pb.nc | (uint64_t)(dp.pb.nm > 0) << 2 | (uint64_t)dp.pb.patchLimit << 4 |
                              (uint64_t)ilog2((uint64_t)cw * ch) << 12 | (uint64_t)ilog2(ntargets) << 18;
     // The persistent pass (one cooperative launch per pass and grid class,
-    // grid barriers between batches) is the default; the proposal network
-    // and graph capture keep one launch per batch.  Its warps per CTA are
-    // tuned across calls (its barrier cost grows with the CTA count, so the
-    // per-batch tuning does not carry over): see persistent_warps.
-    const bool persistentRun = !opt.batchLaunches && !net && !opt.graphs && rs_persistent_supported();
-    int ptrial = -1;
-    int warps = opt.warpsPerBlock ? (int)opt.warpsPerBlock
-                                  : persistentRun ? persistent_warps(tuneKey, ptrial) : tuned_warps(tuneKey);
-    cudaEvent_t ptev[2] = {};
+    // grid barriers between batches) or one launch per batch: chosen per
+    // problem class across calls (launch_config), unless the caller fixes
+    // it; the proposal network and graph capture keep one launch per batch.
+    bool persistentRun = opt.batchLaunches != 1 && !net && !opt.graphs && rs_persistent_supported();
+    int warps = 0;
+    launchKey = tuneKey;
+    if (persistentRun && !opt.warpsPerBlock && opt.batchLaunches == 0) {
+      bool trial = false;
+      launchCfg = launch_config(tuneKey, trial);
+      if (!trial) launchCfg = -1 - launchCfg;   // settled: nothing to record
+      const int c = launchCfg >= 0 ? launchCfg : -1 - launchCfg;
+      persistentRun = c != kPerBatch;
+      warps = c == kPersistent16 ? 16 : c == kPersistent8 ? 8 : tuned_warps(tuneKey);
+    } else {
+      warps = opt.warpsPerBlock ? (int)opt.warpsPerBlock : persistentRun ? 16 : tuned_warps(tuneKey);
+    }
+    stats.launchMode = !persistentRun ? kPerBatch : warps == 16 ? kPersistent16 : warps == 8 ? kPersistent8 : 3;
     // Large problems whose corpus is read from global memory share their
     // random probes within groups of 16 consecutive batch slots: a CTA's warps
     // then read the same corpus windows (cache reuse; heal4096 18 % faster,
@@ -1178,11 +1191,6 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
         };
         wa.gbar = gbar;
         wa.barTimeoutNs = kBarrierTimeoutNs;
-        const bool timed = ptrial >= 0 && pass == 1;
-        if (timed) {
-          for (auto& e : ptev) CK(cudaEventCreate(&e));
-          CK(cudaEventRecord(ptev[0], s));
-        }
         for (int b = singleEnd; b < nbatches;) {
           const int cls = gridClass(b);
           int e = b + 1;
@@ -1198,7 +1206,6 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
           launches++;
           b = e;
         }
-        if (timed) CK(cudaEventRecord(ptev[1], s));
       }
       cudaGraphExec_t passExec = nullptr;
       if (graphPass) {
@@ -1215,15 +1222,6 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       wait_stream(st, epass, cancel);
       if (passExec) cudaGraphExecDestroy(passExec);
       if (hc.error) return fail(RESYNTH_ERROR_DEVICE, "wavefront kernel reported error %u", hc.error);
-      if (ptev[0]) {
-        float t = 0;
-        CK(cudaEventElapsedTime(&t, ptev[0], ptev[1]));
-        persistent_result(tuneKey, ptrial, t);
-        for (auto& e : ptev) {
-          cudaEventDestroy(e);
-          e = nullptr;
-        }
-      }
       if (tuning) {
         float t[3];
         for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&t[i], tev[i], tev[i + 1]));
@@ -1277,6 +1275,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, e0, e1));
   stats.deviceMs = ms;
+  if (launchCfg >= 0 && !*cancel && !*st.abortHost) launch_result(launchKey, launchCfg, ms);
   stats.launches += launches;
   stats.h2dBytes += h2d;
   cudaEventDestroy(e0);
@@ -1505,7 +1504,7 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
   std::vector<rs::WaveArgs> hJobs;
   // Persistent passes (one cooperative launch per pixel layout and pass), or
   // one launch per step with options->batchLaunches.
-  const bool persistent = !opt.batchLaunches && rs_persistent_supported();
+  const bool persistent = opt.batchLaunches != 1 && rs_persistent_supported();
   rs::GridBar* gbar = ar.alloc<rs::GridBar>(1);
   CK(cudaMemsetAsync(gbar, 0, sizeof(rs::GridBar), s));
   unsigned* barErr = reinterpret_cast<unsigned*>(st.hostInts + 8);   // pinned: read back with the counters

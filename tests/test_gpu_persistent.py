@@ -44,7 +44,8 @@ def _case(name):
 def test_persistent_pass_equals_batch_launches(name, warps):
     t, c, spec, kw = _case(name)
     fmt = R.format_indices(*spec)
-    a = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=warps))
+    a = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=warps,
+                                                           batchLaunches=2))
     b = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, warpsPerBlock=warps,
                                                            batchLaunches=1))
     assert a.rc == b.rc == 0, R.last_error()
@@ -59,7 +60,8 @@ def test_persistent_launch_count_render1024():
     """render1024: the whole synthesis in a few dozen launches (one persistent
     launch per pass plus the per-pass bucketing), with the pinned output."""
     t, c, spec, kw = G.wave_workload("render1024")
-    r = R.engine(t, c, R.format_indices(*spec), R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
+    r = R.engine(t, c, R.format_indices(*spec), R.params(**kw),
+                 opts=R.options(mode=R.MODE_WAVEFRONT, batchLaunches=2))
     assert r.rc == 0
     sha, npass, nbetter = G.WAVE_FULL["render1024"]
     assert hashlib.sha256(r.out.tobytes()).hexdigest() == sha
@@ -84,8 +86,23 @@ def test_persistent_cancel_mid_pass():
     call returns 0 (the reference's rule) and the engine stays usable."""
     t, c, spec, kw = _case("heal")
     fmt = R.format_indices(*spec)
-    r = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT), cancel=1)
+    r = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, batchLaunches=2), cancel=1)
     assert r.rc == 0
-    again = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
+    again = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, batchLaunches=2))
     ref = R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT, batchLaunches=1))
     assert again.rc == 0 and np.array_equal(again.out, ref.out)
+
+
+def test_launch_configuration_tuned_across_calls():
+    """Without a fixed launch mode the first three calls of a problem class
+    try the persistent pass with 16 and 8 warps per CTA and one launch per
+    batch; later calls use the fastest.  Every call gives the same output."""
+    t, c, spec, kw = _case("render_tiled")
+    kw = dict(kw, patchSize=12)                       # a class no other test uses
+    fmt = R.format_indices(*spec)
+    runs = [R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT)) for _ in range(5)]
+    assert all(r.rc == 0 for r in runs)
+    assert all(np.array_equal(r.out, runs[0].out) for r in runs[1:])
+    launches = [r.stats["launches"] for r in runs]
+    assert launches[0] < launches[2]                  # persistent, then one launch per batch
+    assert launches[3] == launches[4] and launches[3] in launches[:3]
