@@ -696,21 +696,26 @@ void set_tuned_warps(uint64_t key, int warps) {
 }
 
 // How a problem class's passes are launched, tuned across calls: the first
-// three calls of a class (colour and map channels, patch size, corpus and
-// target sizes) run the persistent pass with 16 warps per CTA, with 8, and
-// one launch per batch; each records the synthesis's device time, and later
-// calls use the fastest.  The persistent pass saves a launch per batch but
+// six calls of a class (colour and map channels, patch size, corpus and
+// target sizes) run, twice in turn, the persistent pass with 16 warps per
+// CTA, with 8, and one launch per batch; each records the synthesis's device
+// time, and later calls use the configuration with the least of its two times
+// (the first use of a configuration in a process also pays for loading its
+// kernels, which the second does not).  The persistent pass saves a launch per batch but
 // pays a grid barrier per batch, and with fewer warps per CTA more CTAs meet
 // at each barrier, so which wins depends on the problem (texture synthesis
 // with many small batches gains most from it).  The output does not depend on
 // the choice.
 enum LaunchConfig { kPersistent16 = 0, kPersistent8 = 1, kPerBatch = 2, kLaunchConfigs = 3 };
+constexpr int kLaunchSamples = 2;
 struct LaunchTune {
   int trials = 0, best = -1;
-  double ms[kLaunchConfigs] = {0, 0, 0};
+  double ms[kLaunchConfigs] = {1e30, 1e30, 1e30};
 };
 std::map<uint64_t, LaunchTune> g_launchTune;
 
+// The configuration of this call; `trial` when its time is to be recorded
+// (the value returned is then the trial number, config = trial % 3).
 int launch_config(uint64_t key, bool& trial) {
   std::lock_guard<std::mutex> lock(g_tuneMu);
   LaunchTune& t = g_launchTune[key];
@@ -718,12 +723,13 @@ int launch_config(uint64_t key, bool& trial) {
   return trial ? t.trials : t.best;
 }
 
-void launch_result(uint64_t key, int config, double ms) {
+void launch_result(uint64_t key, int trialNo, double ms) {
   std::lock_guard<std::mutex> lock(g_tuneMu);
   LaunchTune& t = g_launchTune[key];
-  if (t.best >= 0 || config != t.trials) return;   // another call of the class got there first
-  t.ms[config] = ms;
-  if (++t.trials == kLaunchConfigs) {
+  if (t.best >= 0 || trialNo != t.trials) return;   // another call of the class got there first
+  double& m = t.ms[trialNo % kLaunchConfigs];
+  m = std::min(m, ms);
+  if (++t.trials == kLaunchConfigs * kLaunchSamples) {
     t.best = 0;
     for (int c = 1; c < kLaunchConfigs; c++)
       if (t.ms[c] < t.ms[t.best]) t.best = c;
@@ -1056,7 +1062,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
       bool trial = false;
       launchCfg = launch_config(tuneKey, trial);
       if (!trial) launchCfg = -1 - launchCfg;   // settled: nothing to record
-      const int c = launchCfg >= 0 ? launchCfg : -1 - launchCfg;
+      const int c = (launchCfg >= 0 ? launchCfg : -1 - launchCfg) % kLaunchConfigs;
       persistentRun = c != kPerBatch;
       warps = c == kPersistent16 ? 16 : c == kPersistent8 ? 8 : tuned_warps(tuneKey);
     } else {

@@ -94,15 +94,17 @@ def test_persistent_cancel_mid_pass():
 
 
 def test_launch_configuration_tuned_across_calls():
-    """Without a fixed launch mode the first three calls of a problem class
-    try the persistent pass with 16 and 8 warps per CTA and one launch per
-    batch; later calls use the fastest.  Every call gives the same output."""
+    """Without a fixed launch mode the first six calls of a problem class try,
+    twice in turn, the persistent pass with 16 and 8 warps per CTA and one
+    launch per batch; later calls use the fastest.  Every call gives the same
+    output."""
     t, c, spec, kw = _case("render_tiled")
     kw = dict(kw, patchSize=12)                       # a class no other test uses
     fmt = R.format_indices(*spec)
-    runs = [R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT)) for _ in range(5)]
+    runs = [R.engine(t, c, fmt, R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT)) for _ in range(8)]
     assert all(r.rc == 0 for r in runs)
     assert all(np.array_equal(r.out, runs[0].out) for r in runs[1:])
-    launches = [r.stats["launches"] for r in runs]
-    assert launches[0] < launches[2]                  # persistent, then one launch per batch
-    assert launches[3] == launches[4] and launches[3] in launches[:3]
+    modes = [r.stats["launchMode"] for r in runs]
+    assert modes[:6] == [0, 1, 2, 0, 1, 2]            # persistent 16 and 8 warps, one launch per batch, twice
+    assert modes[6] == modes[7] and modes[6] in (0, 1, 2)
+    assert runs[0].stats["launches"] < runs[2].stats["launches"]
