@@ -463,6 +463,7 @@ def energy_vs_reference(e_gpu: float, ref: dict) -> dict:
          "cpu_mt_energies": mt, "cpu_mt_mean": mt_mean,
          "gpu_over_mt_mean": e_gpu / mt_mean if mt_mean else None,
          "mt_spread": (max(mt) - min(mt)) / mt_mean if mt_mean else None,
+         "mt_runs_at_or_above_gpu": sum(1 for m in mt if m >= e_gpu) if mt else None,
          "cpu_kind": ref["kind"],
          "gate": "wavefront energy at most 1.01 x the threaded reference's mean (one-sided: lower is better)"}
     if mt_mean:
@@ -696,7 +697,7 @@ def main():
                     help="render1024 (default), heal256, heal4096, mapstyle2048, batchN")
     ap.add_argument("--quality", action="store_true", help="energy against the CPU engine instead of speed")
     ap.add_argument("--quality-runs", type=int, default=3)
-    ap.add_argument("--mt-runs", type=int, default=3, help="threaded CPU runs for the energy gate")
+    ap.add_argument("--mt-runs", type=int, default=6, help="threaded CPU runs for the energy gate")
     ap.add_argument("--concurrency", type=int, default=8, help="host workers for batch workloads")
     ap.add_argument("--learned", action="store_true", help="learned proposals against the plain search")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain object of the bench line")
