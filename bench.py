@@ -48,12 +48,14 @@ def term_ops(nc: int, nm: int) -> int:
     per colour and map channel."""
     return 4 + 3 * (nc + nm)
 
-# DRAM bytes (read + write) per k_wave launch, the mean over one synthesis, from
-# an ncu launch list (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of
-#   python bench.py --profile-once --no-cpu --warps 16 --workload W
+# DRAM bytes (read + write) per launch of the wavefront synthesis kernel, the
+# mean over the launches of one synthesis, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/k_wave_persistent_render1024.md):
+#   ncu --set full --clock-control none -k regex:k_wave_persistent -s 6 -c 6 \
+#       python bench.py --profile-once --no-cpu --no-extra --warps 16
 # ncu flushes the caches before each launch, so these are cold-cache figures:
 # an upper bound for the warm launches timed here.
-WAVE_DRAM_BYTES = {}
+WAVE_DRAM_BYTES = {"render1024": 12.84e6}
 SAMPLE_SIDE = 256                 # CPU sample: 256x256 target from the same tile
 
 
