@@ -1547,34 +1547,59 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
     }
     CK(cudaMemcpyAsync(dBands, hb, jobs.size() * 2 * kMaxBands * sizeof(int), cudaMemcpyHostToDevice, s));
     h2d += jobs.size() * 2 * kMaxBands * sizeof(int);
-    // Per-request preparation of the pass on the side streams (every buffer
-    // it touches was allocated, and the boundaries uploaded, on s before the
-    // fork).
-    st.fork_side();
-    for (size_t ai = 0; ai < act.size(); ai++) {
-      const size_t i = act[ai];
-      const cudaStream_t q = st.side[ai % Stream::kSide];
+    // Every active request's bucketing of the pass (and its pass-0 cell
+    // minima) in five launches: the requests' entries go up in one copy.
+    std::vector<rs::PrepJob> pj;
+    std::vector<int> chunk0;
+    int totalChunks = 0, maxKeys = 1, maxCells = 0;
+    pj.reserve(act.size());
+    for (size_t i : act) {
       BatchJob& J = jobs[i];
       const int k = J.k;
-      const unsigned end = J.ends[pass];
       const int nb = (int)J.bandEnds.size();
-      CK(rs_prep_batches(J.dTargets, (int)J.ntargets, (int)J.w, (int)end, 1, J.wa.seed ^ 0x5bd1e995u, J.dBandEnds,
-                         J.dBandPhased, nb, k, J.work, J.batchStart, J.dPass, pass == 0 ? J.vis : nullptr, q));
-      launches += 4;
+      const int nkeys = nb * k * k, nchunks = rs_prep_chunks((int)J.ntargets);
+      const size_t cells = (size_t)nkeys * nchunks;
+      rs::PrepJob P{};
+      P.targets = J.dTargets;
+      P.n = (int)J.ntargets;
+      P.tw = (int)J.w;
+      P.th = (int)J.h;
+      P.endRank = (int)J.ends[pass];
+      P.randomOrder = 1;
+      P.seed = J.wa.seed ^ 0x5bd1e995u;
+      P.bandEnds = J.dBandEnds;
+      P.bandPhased = J.dBandPhased;
+      P.nbands = nb;
+      P.k = k;
+      P.counts = J.work;
+      P.offsets = J.work + cells;
+      P.keys = J.work + 2 * cells + 1;
+      P.nchunks = nchunks;
+      P.batchStart = J.batchStart;
+      P.out = J.dPass;
+      P.vis = pass == 0 ? J.vis : nullptr;
+      P.cellMin = pass == 0 ? J.cellMin : nullptr;
+      chunk0.push_back(totalChunks);
+      totalChunks += nchunks;
+      maxKeys = std::max(maxKeys, nkeys);
+      if (P.cellMin) maxCells = std::max(maxCells, J.cellsW * J.cellsH);
+      pj.push_back(P);
       J.wa.inPlace = (J.tiled || pass > 0) ? 0 : 1;
-      J.wa.pb.cellMin = nullptr;
-      if (pass == 0 && J.cellMin) {
-        CK(rs_cell_min(J.vis, (int)J.w, (int)J.h, J.cellMin, q));
-        launches++;
-        J.wa.pb.cellMin = J.cellMin;
+      J.wa.pb.cellMin = P.cellMin;
+      if (P.cellMin) {
         J.wa.pb.cellsW = J.cellsW;
         J.wa.pb.cellsH = J.cellsH;
       }
       J.wa.pass = (unsigned)pass;
       J.wa.sparse = (pass == 0 && J.noContext && !J.tiled) ? 1 : 0;
-      J.wa.nbatches = nb * k * k;
+      J.wa.nbatches = nkeys;
     }
-    st.join_side();
+    chunk0.push_back(totalChunks);
+    const rs::PrepJob* dPJ = ar.upload(pj.data(), pj.size(), h2d);
+    const int* dChunk0 = ar.upload(chunk0.data(), chunk0.size(), h2d);
+    const int cellBlocks = maxCells ? std::min(64, (maxCells + 7) / 8) : 0;
+    CK(rs_prep_batches_multi(dPJ, dChunk0, (int)pj.size(), totalChunks, maxKeys, cellBlocks, s));
+    launches += cellBlocks ? 5 : 4;
     // requests grouped by pixel layout, one launch per group per step
     std::map<std::pair<int, int>, std::vector<size_t>> groups;
     for (size_t i : act) groups[{jobs[i].dp.pb.nc, jobs[i].dp.pb.nm > 0 ? 1 : 0}].push_back(i);

@@ -120,6 +120,26 @@ struct WaveArgs {
   long long barTimeoutNs;        // a barrier wait longer than this gives up (kErrBarrier)
 };
 
+// One request's bucketing of a pass, for rs_prep_batches_multi (the
+// arguments of rs_prep_batches with its work split out; cellMin non-null =
+// also the pass-0 cell minima of vis).
+struct PrepJob {
+  const int2* targets;
+  int n, tw, th, endRank, randomOrder;
+  uint32_t seed;
+  const int* bandEnds;
+  const int* bandPhased;
+  int nbands, k;
+  int* keys;
+  int* counts;
+  int* offsets;
+  int nchunks;
+  int* batchStart;
+  int2* out;
+  int* vis;
+  int* cellMin;
+};
+
 // Frozen-state scoring and energy.
 struct ScoreArgs {
   Problem pb;
@@ -176,6 +196,14 @@ cudaError_t rs_prep_batches(const int2* targets, int n, int tw, int endRank, int
                             const int* dBandEnds, const int* dBandPhased, int nbands, int k, int* work,
                             int* batchStart, int2* out, int* vis, cudaStream_t s);
 size_t rs_prep_batches_ints(int n, int nkeys);
+// rs_prep_batches (and pass-0 cell minima) for njobs requests in five launches:
+// dJobs[njobs] in device memory, dChunk0[j] = the first bucketing chunk of
+// request j (chunks of rs_prep_chunks(n) each, totalChunks in all), maxKeys =
+// the largest nbands * k * k, cellBlocks = CTAs per request for the cell
+// minima (0 = none).
+cudaError_t rs_prep_batches_multi(const rs::PrepJob* dJobs, const int* dChunk0, int njobs, int totalChunks,
+                                  int maxKeys, int cellBlocks, cudaStream_t s);
+int rs_prep_chunks(int n);
 cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, size_t maskRow, const uint8_t* mask2,
                      size_t mask2Row, int w, int h, int bpp, uint8_t* target, uint8_t* corpus, cudaStream_t s);
 cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow, cudaStream_t s);

@@ -155,14 +155,12 @@ constexpr int kBucketChunk = 8192;
 // rank >= endRank are not visited this pass.  key = band * K + phase.  Each
 // CTA counts its chunk's keys; counts are stored key-major, [key][chunk], so
 // one exclusive scan gives every (key, chunk) its output position.
-__global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
-                             const int* bandEnds, const int* bandPhased, int nbands, int k, int* keys, int* counts,
-                             int nchunks, int* vis) {
-  extern __shared__ int hist[];
+__device__ void batch_keys_chunk(int chunk, const int2* targets, int n, int tw, int endRank, int randomOrder,
+                                 uint32_t seed, const int* bandEnds, const int* bandPhased, int nbands, int k,
+                                 int* keys, int* counts, int nchunks, int* vis, int* hist) {
   const int nkeys = nbands * k * k;
   for (int i = threadIdx.x; i < nkeys; i += blockDim.x) hist[i] = 0;
   __syncthreads();
-  const int chunk = blockIdx.x;
   for (int i = threadIdx.x; i < kBucketChunk; i += blockDim.x) {
     const int t = chunk * kBucketChunk + i;
     if (t >= n) break;
@@ -185,9 +183,17 @@ __global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, in
   for (int i = threadIdx.x; i < nkeys; i += blockDim.x) counts[(size_t)i * nchunks + chunk] = hist[i];
 }
 
+__global__ void k_batch_keys(const int2* targets, int n, int tw, int endRank, int randomOrder, uint32_t seed,
+                             const int* bandEnds, const int* bandPhased, int nbands, int k, int* keys, int* counts,
+                             int nchunks, int* vis) {
+  extern __shared__ int hist[];
+  batch_keys_chunk(blockIdx.x, targets, n, tw, endRank, randomOrder, seed, bandEnds, bandPhased, nbands, k, keys,
+                   counts, nchunks, vis, hist);
+}
+
 // Exclusive scan of n ints by one CTA of 1024 threads, 8 consecutive
 // elements per thread per round; offsets[n] = the total.
-__global__ void __launch_bounds__(1024) k_scan_wide(const int* counts, int n, int* offsets) {
+__device__ void scan_wide(const int* counts, int n, int* offsets) {
   __shared__ int warpSums[32];
   __shared__ int carry;
   constexpr int kPer = 8;
@@ -233,6 +239,10 @@ __global__ void __launch_bounds__(1024) k_scan_wide(const int* counts, int n, in
   if (threadIdx.x == 0) offsets[n] = carry;
 }
 
+__global__ void __launch_bounds__(1024) k_scan_wide(const int* counts, int n, int* offsets) {
+  scan_wide(counts, n, offsets);
+}
+
 // batchStart[key] = the scanned offset of (key, chunk 0).
 __global__ void k_batch_starts(const int* offsets, int nkeys, int nchunks, int* batchStart) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= nkeys; i += gridDim.x * blockDim.x)
@@ -243,12 +253,11 @@ __global__ void k_batch_starts(const int* offsets, int nkeys, int nchunks, int* 
 // list.  Each CTA places its chunk; a lane's position is its (key, chunk)
 // offset + the same-key count of earlier warps (taken warp by warp) + its
 // rank among the same-key lanes of its warp.
-__global__ void k_scatter(const int2* targets, int n, const int* keys, const int* offsets, int nkeys, int nchunks,
-                          int2* out) {
-  extern __shared__ int cnt[];
+__device__ void scatter_chunk(int chunk, const int2* targets, int n, const int* keys, const int* offsets, int nkeys,
+                              int nchunks, int2* out, int* cnt) {
   for (int i = threadIdx.x; i < nkeys; i += blockDim.x) cnt[i] = 0;
   __syncthreads();
-  const int chunk = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   unsigned lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
   for (int base = 0; base < kBucketChunk; base += blockDim.x) {
@@ -267,6 +276,51 @@ __global__ void k_scatter(const int2* targets, int n, const int* keys, const int
     }
     if (key >= 0) out[offsets[(size_t)key * nchunks + chunk] + before + __popc(peers & lt)] = targets[t];
   }
+}
+
+__global__ void k_scatter(const int2* targets, int n, const int* keys, const int* offsets, int nkeys, int nchunks,
+                          int2* out) {
+  extern __shared__ int cnt[];
+  scatter_chunk(blockIdx.x, targets, n, keys, offsets, nkeys, nchunks, out, cnt);
+}
+
+// The same bucketing for many requests at once: one launch per stage, each
+// request's chunks (or, for the scans, one CTA) found from its entry.
+__device__ __forceinline__ int job_of_chunk(const int* chunk0, int njobs, int c) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (chunk0[mid] <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_batch_keys_multi(const PrepJob* jobs, const int* chunk0, int njobs) {
+  extern __shared__ int hist[];
+  const int j = job_of_chunk(chunk0, njobs, blockIdx.x);
+  const PrepJob& J = jobs[j];
+  batch_keys_chunk(blockIdx.x - chunk0[j], J.targets, J.n, J.tw, J.endRank, J.randomOrder, J.seed, J.bandEnds,
+                   J.bandPhased, J.nbands, J.k, J.keys, J.counts, J.nchunks, J.vis, hist);
+}
+
+__global__ void __launch_bounds__(1024) k_scan_wide_multi(const PrepJob* jobs) {
+  const PrepJob& J = jobs[blockIdx.x];
+  scan_wide(J.counts, J.nbands * J.k * J.k * J.nchunks, J.offsets);
+}
+
+__global__ void k_batch_starts_multi(const PrepJob* jobs) {
+  const PrepJob& J = jobs[blockIdx.x];
+  const int nkeys = J.nbands * J.k * J.k;
+  for (int i = threadIdx.x; i <= nkeys; i += blockDim.x) J.batchStart[i] = J.offsets[(size_t)i * J.nchunks];
+}
+
+__global__ void k_scatter_multi(const PrepJob* jobs, const int* chunk0, int njobs) {
+  extern __shared__ int cnt[];
+  const int j = job_of_chunk(chunk0, njobs, blockIdx.x);
+  const PrepJob& J = jobs[j];
+  scatter_chunk(blockIdx.x - chunk0[j], J.targets, J.n, J.keys, J.offsets, J.nbands * J.k * J.k, J.nchunks, J.out,
+                cnt);
 }
 
 int blocks_for(int n, int per) { return (n + per - 1) / per; }
@@ -347,10 +401,10 @@ __global__ void k_vis_to_has(const int* vis, int npx, uint8_t* has) {
 }
 // Least visit stamp of each kCell x kCell cell: a pixel of the cell can have
 // a value during batch b only if the cell's minimum is below b.
-__global__ void k_cell_min(const int* vis, int tw, int th, int* cellMin) {
+__device__ void cell_min(const int* vis, int tw, int th, int* cellMin, int first, int step) {
   const int cw = (tw + kCell - 1) >> kCellShift, ch = (th + kCell - 1) >> kCellShift;
   const int lane = threadIdx.x & 31;
-  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < cw * ch; c += (gridDim.x * blockDim.x) >> 5) {
+  for (int c = first; c < cw * ch; c += step) {
     const int x0 = (c % cw) << kCellShift, y0 = (c / cw) << kCellShift;
     int m = 0x7fffffff;
     for (int i = lane; i < kCell * kCell; i += 32) {
@@ -360,6 +414,19 @@ __global__ void k_cell_min(const int* vis, int tw, int th, int* cellMin) {
     for (int o = 16; o; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
     if (lane == 0) cellMin[c] = m;
   }
+}
+
+__global__ void k_cell_min(const int* vis, int tw, int th, int* cellMin) {
+  cell_min(vis, tw, th, cellMin, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
+}
+
+// Cell minima of many requests: blockIdx.y is the request (those without a
+// cell grid have cellMin == null).
+__global__ void k_cell_min_multi(const PrepJob* jobs) {
+  const PrepJob& J = jobs[blockIdx.y];
+  if (!J.cellMin) return;
+  cell_min(J.vis, J.tw, J.th, J.cellMin, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+           (gridDim.x * blockDim.x) >> 5);
 }
 }  // namespace
 }  // namespace rs
@@ -678,3 +745,17 @@ extern "C" cudaError_t rs_order_finish(int type, const int2* targets, int n, int
   k_order_gather<<<grid_of(n), 256, 0, s>>>(targets, va, perm, n, out);
   return cudaGetLastError();
 }
+
+extern "C" cudaError_t rs_prep_batches_multi(const PrepJob* dJobs, const int* dChunk0, int njobs, int totalChunks,
+                                             int maxKeys, int cellBlocks, cudaStream_t s) {
+  if (njobs < 1) return cudaSuccess;
+  const size_t smem = (size_t)maxKeys * sizeof(int);
+  k_batch_keys_multi<<<totalChunks, 256, smem, s>>>(dJobs, dChunk0, njobs);
+  k_scan_wide_multi<<<njobs, 1024, 0, s>>>(dJobs);
+  k_batch_starts_multi<<<njobs, 256, 0, s>>>(dJobs);
+  k_scatter_multi<<<totalChunks, 256, smem, s>>>(dJobs, dChunk0, njobs);
+  if (cellBlocks > 0) k_cell_min_multi<<<dim3(cellBlocks, njobs), 256, 0, s>>>(dJobs);
+  return cudaGetLastError();
+}
+
+extern "C" int rs_prep_chunks(int n) { return std::max(1, blocks_for(n, kBucketChunk)); }
