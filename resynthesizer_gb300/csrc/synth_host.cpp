@@ -1309,7 +1309,6 @@ struct BatchJob {
   uint8_t* dT = nullptr;
   DeviceProblem dp;
   int2* dTargets = nullptr;
-  int* dCounts = nullptr;
   int2* cpts = nullptr;
   unsigned ntargets = 0, ends[rs::kPasses] = {}, estimated = 0;
   bool noContext = true, tiled = false, active = false;
@@ -1324,6 +1323,7 @@ struct BatchJob {
   std::vector<int> bandEnds;
   rs::WaveArgs wa{};
   unsigned bettersTotal = 0, passes = 0;
+  int setupIdx = -1;             // entry in the call's set-up list (-1: failed a host check)
 };
 
 bool batch_eligible(const TResynthRequest& r, const TResynthOptions& opt) {
@@ -1363,7 +1363,11 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
   st.fork_side();
   for (int q = 0; q < Stream::kSide; q++) side.a.emplace_back(new Arena(st.side[q], (size_t)64 << 20, s));
   int nextSide = 0;
-  // 1. host checks (the reference's order), upload, adaption, preparation
+  std::vector<rs::SetupJob> setup;
+  std::vector<int> setupChunk0;
+  int setupChunks = 0, maxPx = 1;
+  std::map<std::pair<double, double>, const uint32_t*> tables;   // metric tables by (sensitivity, mapWeight)
+  // 1. host checks (the reference's order), upload
   for (size_t i = 0; i < reqs.size(); i++) {
     BatchJob& J = jobs[i];
     TResynthRequest& R = *reqs[i];
@@ -1404,6 +1408,9 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       R.result = IMAGE_SYNTH_ERROR_EMPTY_CORPUS;
       continue;
     }
+    // Buffers from the side arenas, the caller's buffers uploaded as they are
+    // (row padding included) on the side streams; the set-up kernels below
+    // serve every request at once.
     const int sq = nextSide++ % Stream::kSide;
     const cudaStream_t q = st.side[sq];
     Arena& qa = *side.a[sq];
@@ -1420,47 +1427,111 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
       CK(cudaMemcpyAsync(dMask2, R.mask2->data, m2Bytes, cudaMemcpyHostToDevice, q));
       h2d += m2Bytes;
     }
-    J.dT = qa.alloc<uint8_t>((size_t)w * h * d);
-    uint8_t* dC = qa.alloc<uint8_t>((size_t)w * h * d);
-    CK(rs_adapt(J.dImg, img->rowBytes, dMask, R.mask->rowBytes, dMask2, R.mask2 ? R.mask2->rowBytes : 0, (int)w,
-                (int)h, (int)J.bpp, J.dT, dC, q));
-    const long long maxD2 = wave_radius2((int)w, (int)h);
-    int nWave = 0;
-    const int2* dWave = wave_offsets_device(nWave);
-    const std::vector<int2>& wl = wave_offsets_host();
-    nWave = (int)(std::partition_point(wl.begin(), wl.end(), [&](const int2& o) {
-                    return (long long)o.x * o.x + (long long)o.y * o.y <= maxD2;
-                  }) - wl.begin());
-    const std::vector<int2> noList;
-    J.dp = make_problem(qa, q, J.p, J.f, J.dT, w, h, dC, w, h, nullptr, nullptr, noList, maxD2, h2d, launches, dWave,
-                        nWave);
-    const size_t tn = (size_t)w * h;
-    int* scratch = qa.alloc<int>((size_t)rs_prep_scratch_ints((int)w, (int)h));
-    J.dCounts = qa.alloc<int>(4);
+    const size_t tn = (size_t)w * h, tnPad = (tn + 3) & ~(size_t)3;
+    J.dT = qa.alloc<uint8_t>(tn * d);
+    uint8_t* dC = qa.alloc<uint8_t>(tn * d);
+    rs::Problem& pb = J.dp.pb;
+    pb.tw = pb.cw = (int)w;
+    pb.th = pb.ch = (int)h;
+    pb.nc = J.f.img_match_bpp;
+    pb.nm = 0;
+    J.dp.tpx = qa.alloc<uint32_t>(tn);
+    pb.tpx = J.dp.tpx;
+    pb.cpx = qa.alloc<uint32_t>(tnPad);
+    pb.padW = (int)w + 2 * rs::kPad;
+    pb.cpxPad = qa.alloc<uint32_t>((((size_t)pb.padW * (h + 2 * rs::kPad)) + 3) & ~(size_t)3);
+    pb.has = qa.alloc<uint8_t>(tn);
+    pb.src = qa.alloc<int2>(tn);
+    J.vis = qa.alloc<int>(tn);
+    pb.vis = J.vis;
     J.dTargets = qa.alloc<int2>(tn);
     J.cpts = qa.alloc<int2>(tn);
-    CK(rs_prep_target(J.dT, (int)w, (int)h, J.f.total_bpp, J.f.alpha_bip, J.f.isAlphaTarget ? 1 : 0,
-                      J.p.matchContextType ? 1 : 0, J.dp.pb.has, J.dp.pb.src, scratch, J.dTargets, J.dCounts, q));
-    CK(rs_prep_corpus(dC, (int)w, (int)h, J.f.total_bpp, J.f.alpha_bip, J.f.isAlphaSource ? 1 : 0, scratch, J.cpts,
-                      J.dCounts + 2, q));
-    launches += 8;
+    const long long maxD2 = wave_radius2((int)w, (int)h);
+    int nWave = 0;
+    pb.offs = wave_offsets_device(nWave);
+    const std::vector<int2>& wl = wave_offsets_host();
+    pb.noffs = (int)(std::partition_point(wl.begin(), wl.end(), [&](const int2& o) {
+                       return (long long)o.x * o.x + (long long)o.y * o.y <= maxD2;
+                     }) - wl.begin());
+    pb.boxW = (int)w;
+    pb.boxH = (int)h;
+    pb.maxD2 = maxD2;
+    pb.patchLimit = (int)std::max(J.p.patchSize, 2u);
+    pb.tileH = J.p.isMakeSeamlesslyTileableHorizontally ? 1 : 0;
+    pb.tileV = J.p.isMakeSeamlesslyTileableVertically ? 1 : 0;
+    uint32_t ct[512], mt[512];
+    metric_tables(J.p.sensitivityToOutliers, J.p.mapWeight, ct, mt);
+    pb.clipCost = 65535u * J.f.img_match_bpp;
+    const auto key = std::make_pair(J.p.sensitivityToOutliers, J.p.mapWeight);
+    auto tab = tables.find(key);
+    if (tab == tables.end()) {
+      uint32_t both[1024];
+      std::copy(ct, ct + 512, both);
+      std::copy(mt, mt + 512, both + 512);
+      const uint32_t* dTab = qa.upload(both, 1024, h2d);
+      tab = tables.emplace(key, dTab).first;
+    }
+    pb.ctab = tab->second;
+    pb.mtab = tab->second + 512;
+    rs::SetupJob S{};
+    S.img = J.dImg;
+    S.imgRow = img->rowBytes;
+    S.mask = dMask;
+    S.maskRow = R.mask->rowBytes;
+    S.mask2 = dMask2;
+    S.mask2Row = R.mask2 ? R.mask2->rowBytes : 0;
+    S.w = (int)w;
+    S.h = (int)h;
+    S.bpp = (int)J.bpp;
+    S.nc = J.f.img_match_bpp;
+    S.alpha = J.f.alpha_bip;
+    S.alphaT = J.f.isAlphaTarget ? 1 : 0;
+    S.alphaS = J.f.isAlphaSource ? 1 : 0;
+    S.useContext = J.p.matchContextType ? 1 : 0;
+    S.target = J.dT;
+    S.corpus = dC;
+    S.tpx = pb.tpx;
+    S.cpx = const_cast<uint32_t*>(pb.cpx);
+    S.cpxPad = const_cast<uint32_t*>(pb.cpxPad);
+    S.padW = pb.padW;
+    S.has = pb.has;
+    S.src = pb.src;
+    S.vis = J.vis;
+    S.targets = J.dTargets;
+    S.cpts = J.cpts;
+    S.chunk0 = setupChunks;
+    J.setupIdx = (int)setup.size();
+    setup.push_back(S);
+    setupChunk0.push_back(setupChunks);
+    setupChunks += rs_setup_chunks((int)tn);
+    maxPx = std::max(maxPx, (int)std::max(tn, (size_t)pb.padW * (h + 2 * rs::kPad)));
   }
   st.join_side();
-  // 2. target and corpus counts of every request: one synchronisation
-  std::vector<int> counts(4 * jobs.size(), 0);
-  for (size_t i = 0; i < jobs.size(); i++)
-    if (jobs[i].dCounts) CK(cudaMemcpyAsync(&counts[4 * i], jobs[i].dCounts, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  // 2. every request's adaption, packing, initial state and compaction in
+  // four launches; their target and corpus counts in one read-back
+  setupChunk0.push_back(setupChunks);
+  rs::SetupJob* dSetup = setup.empty() ? nullptr : ar.upload(setup.data(), setup.size(), h2d);
+  const int* dSetupChunk0 = setup.empty() ? nullptr : ar.upload(setupChunk0.data(), setupChunk0.size(), h2d);
+  int* dCountsAll = ar.alloc<int>(4 * std::max<size_t>(1, setup.size()));
+  int* setupWork = ar.alloc<int>(rs_setup_work_ints(setupChunks, (int)setup.size()) + 1);
+  CK(rs_setup_multi(dSetup, dSetupChunk0, (int)setup.size(), setupChunks, maxPx, dCountsAll, setupWork, s));
+  launches += setup.empty() ? 0 : 4;
+  std::vector<int> countsAll(4 * setup.size(), 0);
+  if (!setup.empty())
+    CK(cudaMemcpyAsync(countsAll.data(), dCountsAll, countsAll.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  d2h += countsAll.size() * sizeof(int);
   rs::Counters* ctrs = ar.alloc<rs::Counters>(jobs.size());
   CK(cudaMemsetAsync(ctrs, 0, jobs.size() * sizeof(rs::Counters), s));
   // every request's band boundaries and phase flags, uploaded once per pass
   int* dBands = ar.alloc<int>(jobs.size() * 2 * kMaxBands);
   for (size_t i = 0; i < jobs.size(); i++) {
     BatchJob& J = jobs[i];
-    if (!J.dCounts) continue;
-    J.ntargets = (unsigned)counts[4 * i];
-    J.noContext = counts[4 * i + 1] == 0;
-    const int ncorpus = counts[4 * i + 2];
+    if (J.setupIdx < 0) continue;
+    const int* c = &countsAll[4 * (size_t)J.setupIdx];
+    J.ntargets = (unsigned)c[0];
+    J.noContext = c[1] == 0;
+    const int ncorpus = c[2];
     if (!J.ntargets) {   // lib/engine.c:605-627
       J.req->result = IMAGE_SYNTH_ERROR_EMPTY_TARGET;
       continue;
@@ -1476,11 +1547,6 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
     pass_schedule(J.ntargets, J.ends, J.estimated);
     J.k = opt.phaseSide ? (int)opt.phaseSide : phase_side_box(wave_offsets_host(), pb.patchLimit, (int)J.w, (int)J.h);
     J.tiled = pb.tileH || pb.tileV;
-    const size_t tn = (size_t)J.w * J.h;
-    J.vis = ar.alloc<int>(tn);
-    CK(rs_vis_init(pb.has, (int)tn, J.vis, s));
-    launches++;
-    pb.vis = J.vis;
     J.cellsW = ((int)J.w + rs::kCell - 1) >> rs::kCellShift;
     J.cellsH = ((int)J.h + rs::kCell - 1) >> rs::kCellShift;
     J.cellMin = J.tiled ? nullptr : ar.alloc<int>((size_t)J.cellsW * J.cellsH);
@@ -1675,14 +1741,23 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
         J.active = false;   // lib/refiner.h:111
     }
   }
-  // 4. results: colours back into the caller's layout, one copy per request
+  // 4. results: the colours of every finished request back into its uploaded
+  // image in one launch, then one copy per request into the caller's buffer
+  bool anyBack = false;
   for (BatchJob& J : jobs) {
-    if (!J.dT || J.req->result) continue;
-    CK(rs_launch_unpack_colors(J.dT, (int)J.w, (int)J.h, J.f.total_bpp, J.f.img_match_bpp, J.dp.tpx, s));
-    CK(rs_unadapt(J.dT, (int)J.w, (int)J.h, (int)J.bpp, J.dImg, J.req->image->rowBytes, s));
+    const bool back = J.setupIdx >= 0 && !J.req->result;
+    if (J.setupIdx >= 0) setup[J.setupIdx].writeBack = back ? 1 : 0;
+    anyBack |= back;
+  }
+  if (anyBack) {
+    CK(cudaMemcpyAsync(dSetup, setup.data(), setup.size() * sizeof(rs::SetupJob), cudaMemcpyHostToDevice, s));
+    CK(rs_writeback_multi(dSetup, (int)setup.size(), maxPx, s));
+    launches++;
+  }
+  for (BatchJob& J : jobs) {
+    if (J.setupIdx < 0 || J.req->result) continue;
     CK(cudaMemcpyAsync(J.req->image->data, J.dImg, J.imgBytes, cudaMemcpyDeviceToHost, s));
     d2h += J.imgBytes;
-    launches += 2;
     stats.passes = std::max(stats.passes, J.passes);
   }
   CK(cudaEventRecord(e1, s));

@@ -140,6 +140,35 @@ struct PrepJob {
   int* cellMin;
 };
 
+// One Simple-API request of the many-request path, for the set-up and
+// write-back kernels that serve every request of a call at once: the caller's
+// buffers (uploaded as they are, row padding included), the interleaved
+// pixmaps the adaption writes, the packed words, the prepared state and the
+// request's first compaction chunk.
+struct SetupJob {
+  const uint8_t* img;
+  size_t imgRow;
+  const uint8_t* mask;
+  size_t maskRow;
+  const uint8_t* mask2;
+  size_t mask2Row;
+  int w, h, bpp;                 // the caller's pixel: bpp bytes
+  int nc, alpha, alphaT, alphaS, useContext;
+  uint8_t* target;               // interleaved pixmaps, bpp + 1 bytes per pixel
+  uint8_t* corpus;
+  uint32_t* tpx;
+  uint32_t* cpx;
+  uint32_t* cpxPad;
+  int padW;
+  uint8_t* has;
+  int2* src;
+  int* vis;
+  int2* targets;
+  int2* cpts;
+  int chunk0;                    // first compaction chunk (rs_setup_chunks(w * h) of them)
+  int writeBack;                 // write-back kernel: 1 = put the colours into img
+};
+
 // Frozen-state scoring and energy.
 struct ScoreArgs {
   Problem pb;
@@ -204,6 +233,17 @@ size_t rs_prep_batches_ints(int n, int nkeys);
 cudaError_t rs_prep_batches_multi(const rs::PrepJob* dJobs, const int* dChunk0, int njobs, int totalChunks,
                                   int maxKeys, int cellBlocks, cudaStream_t s);
 int rs_prep_chunks(int n);
+// The many-request set-up for njobs requests (dJobs in device memory, dChunk0
+// their first chunks, njobs + 1 entries): adaption, packing, initial state and
+// visit stamps, then the compaction of targets and corpus points;
+// counts[4 j .. 4 j + 2] = targets, any context, corpus points of request j
+// (zeroed here).  work: rs_setup_work_ints(totalChunks, njobs) ints.
+cudaError_t rs_setup_multi(const rs::SetupJob* dJobs, const int* dChunk0, int njobs, int totalChunks, int maxPx,
+                           int* counts, int* work, cudaStream_t s);
+int rs_setup_chunks(int npx);
+size_t rs_setup_work_ints(int totalChunks, int njobs);
+// The colours of every request with writeBack set back into its uploaded image.
+cudaError_t rs_writeback_multi(const rs::SetupJob* dJobs, int njobs, int maxPx, cudaStream_t s);
 cudaError_t rs_adapt(const uint8_t* img, size_t imgRow, const uint8_t* mask, size_t maskRow, const uint8_t* mask2,
                      size_t mask2Row, int w, int h, int bpp, uint8_t* target, uint8_t* corpus, cudaStream_t s);
 cudaError_t rs_unadapt(const uint8_t* target, int w, int h, int bpp, uint8_t* img, size_t imgRow, cudaStream_t s);

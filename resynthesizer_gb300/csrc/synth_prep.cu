@@ -759,3 +759,184 @@ extern "C" cudaError_t rs_prep_batches_multi(const PrepJob* dJobs, const int* dC
 }
 
 extern "C" int rs_prep_chunks(int n) { return std::max(1, blocks_for(n, kBucketChunk)); }
+
+// ---------------------------------------------------------------------------
+// The many-request path's set-up and write-back: the same work as rs_adapt,
+// the packing, rs_prep_target, rs_prep_corpus and rs_vis_init, then
+// rs_unadapt, but for every request of a call in a handful of launches
+// (blockIdx.y, or the compaction chunk, says which request).
+namespace rs {
+namespace {
+
+__device__ __forceinline__ int job_of(const int* chunk0, int njobs, int c) { return job_of_chunk(chunk0, njobs, c); }
+
+// Adaption (lib/adaptSimple.h:260-354), packed words, padded corpus, initial
+// hasValue / sourceOf (lib/engine.c:338-391) and visit stamps.
+__global__ void k_setup_pixels(const SetupJob* jobs, int* counts) {
+  const SetupJob& J = jobs[blockIdx.y];
+  const int npx = J.w * J.h, d = J.bpp + 1;
+  int ctx = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npx; i += gridDim.x * blockDim.x) {
+    const int x = i % J.w, y = i / J.w;
+    const uint8_t* src = J.img + (size_t)y * J.imgRow + (size_t)x * J.bpp;
+    const uint8_t m = J.mask[(size_t)y * J.maskRow + x];
+    const uint8_t cm = J.mask2 ? J.mask2[(size_t)y * J.mask2Row + x] : (uint8_t)~m;
+    uint8_t* t = J.target + (size_t)i * d;
+    uint8_t* c = J.corpus + (size_t)i * d;
+    t[0] = m;
+    c[0] = cm;
+    uint32_t tw = m, cw = cm;
+    for (int k = 0; k < J.bpp; k++) {
+      const uint8_t v = src[k];
+      t[1 + k] = c[1 + k] = v;
+      if (k < J.nc) {
+        tw |= (uint32_t)v << (8 * (k + 1));
+        cw |= (uint32_t)v << (8 * (k + 1));
+      }
+    }
+    J.tpx[i] = tw;
+    J.cpx[i] = cw;
+    const bool opaque = !J.alphaT || src[J.alpha - 1] != 0;
+    const uint8_t hv = (J.useContext && m == 0 && opaque) ? 1 : 0;
+    J.has[i] = hv;
+    J.src[i] = make_int2(-1, -1);
+    J.vis[i] = hv ? -1 : 0x7fffffff;
+    ctx |= hv;
+  }
+  // the corpus with a kPad-wide border of masked (zero) words
+  const int pw = J.w + 2 * kPad, ph = J.h + 2 * kPad;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < pw * ph; i += gridDim.x * blockDim.x) {
+    const int x = i % pw - kPad, y = i / pw - kPad;
+    uint32_t word = 0;
+    if (x >= 0 && x < J.w && y >= 0 && y < J.h) {
+      const uint8_t* src = J.img + (size_t)y * J.imgRow + (size_t)x * J.bpp;
+      word = J.mask2 ? J.mask2[(size_t)y * J.mask2Row + x] : (uint8_t)~J.mask[(size_t)y * J.maskRow + x];
+      for (int k = 0; k < J.nc; k++) word |= (uint32_t)src[k] << (8 * (k + 1));
+    }
+    J.cpxPad[i] = word;
+  }
+  ctx = __reduce_or_sync(0xffffffffu, ctx);
+  if ((threadIdx.x & 31) == 0 && ctx) atomicOr(&counts[4 * blockIdx.y + 1], 1);
+}
+
+__device__ __forceinline__ bool setup_target(const SetupJob& J, int i) { return J.target[(size_t)i * (J.bpp + 1)] != 0; }
+__device__ __forceinline__ bool setup_corpus(const SetupJob& J, int i) {
+  const uint8_t* q = J.corpus + (size_t)i * (J.bpp + 1);
+  return q[0] == 0xFF && (!J.alphaS || q[J.alpha] != 0);
+}
+
+// Per compaction chunk: how many targets and corpus points it holds.
+__global__ void k_setup_count(const SetupJob* jobs, const int* chunk0, int njobs, int* cntT, int* cntC) {
+  const int j = job_of(chunk0, njobs, blockIdx.x);
+  const SetupJob& J = jobs[j];
+  const int npx = J.w * J.h, base = (blockIdx.x - chunk0[j]) * kChunk;
+  int a = 0, b = 0;
+  for (int k = 0; k < kItems; k++) {
+    const int i = base + k * kThreads + threadIdx.x;
+    if (i < npx) {
+      a += setup_target(J, i);
+      b += setup_corpus(J, i);
+    }
+  }
+  a = __reduce_add_sync(0xffffffffu, a);
+  b = __reduce_add_sync(0xffffffffu, b);
+  __shared__ int sa[kThreads / 32], sb[kThreads / 32];
+  if ((threadIdx.x & 31) == 0) {
+    sa[threadIdx.x >> 5] = a;
+    sb[threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ta = 0, tb = 0;
+    for (int w = 0; w < kThreads / 32; w++) {
+      ta += sa[w];
+      tb += sb[w];
+    }
+    cntT[blockIdx.x] = ta;
+    cntC[blockIdx.x] = tb;
+  }
+}
+
+// One CTA per request: the exclusive scans of its chunks' counts and the totals.
+__global__ void k_setup_scan(const int* chunk0, const int* cntT, const int* cntC, int* offT, int* offC, int* counts) {
+  __shared__ int warpSums[kThreads / 32];
+  const int j = blockIdx.x, c0 = chunk0[j], nb = chunk0[j + 1] - c0;
+  for (int which = 0; which < 2; which++) {
+    const int* cnt = which ? cntC : cntT;
+    int* off = which ? offC : offT;
+    int carry = 0;
+    for (int b = 0; b < nb; b += kThreads) {
+      const int i = b + threadIdx.x;
+      const int v = i < nb ? cnt[c0 + i] : 0;
+      int total;
+      const int ex = block_exclusive(v, warpSums, total);
+      if (i < nb) off[c0 + i] = carry + ex;
+      carry += total;
+    }
+    if (threadIdx.x == 0) counts[4 * j + (which ? 2 : 0)] = carry;
+    __syncthreads();
+  }
+}
+
+__global__ void k_setup_compact(const SetupJob* jobs, const int* chunk0, int njobs, const int* offT,
+                                const int* offC) {
+  __shared__ int warpSums[kThreads / 32];
+  const int j = job_of(chunk0, njobs, blockIdx.x);
+  const SetupJob& J = jobs[j];
+  const int npx = J.w * J.h, base = (blockIdx.x - chunk0[j]) * kChunk;
+  int pt = offT[blockIdx.x], pc = offC[blockIdx.x];
+  for (int k = 0; k < kItems; k++) {
+    const int i = base + k * kThreads + threadIdx.x;
+    const bool ft = i < npx && setup_target(J, i);
+    const bool fc = i < npx && setup_corpus(J, i);
+    int tt, tc;
+    const int et = block_exclusive(ft ? 1 : 0, warpSums, tt);
+    const int ec = block_exclusive(fc ? 1 : 0, warpSums, tc);
+    if (ft) J.targets[pt + et] = make_int2(i % J.w, i / J.w);
+    if (fc) J.cpts[pc + ec] = make_int2(i % J.w, i / J.w);
+    pt += tt;
+    pc += tc;
+  }
+}
+
+// antiAdaptImage (lib/adaptSimple.h:110-168) for every finished request: the
+// synthesized colours into its uploaded image (the other bytes never change).
+__global__ void k_writeback(const SetupJob* jobs) {
+  const SetupJob& J = jobs[blockIdx.y];
+  if (!J.writeBack) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < J.w * J.h; i += gridDim.x * blockDim.x) {
+    const int x = i % J.w, y = i / J.w;
+    uint8_t* o = const_cast<uint8_t*>(J.img) + (size_t)y * J.imgRow + (size_t)x * J.bpp;
+    const uint32_t w = J.tpx[i];
+    for (int k = 0; k < J.nc; k++) o[k] = (uint8_t)(w >> (8 * (k + 1)));
+  }
+}
+
+}  // namespace
+}  // namespace rs
+
+extern "C" int rs_setup_chunks(int npx) { return std::max(1, blocks_for(npx, kChunk)); }
+extern "C" size_t rs_setup_work_ints(int totalChunks, int njobs) { return 4 * (size_t)totalChunks + 2 * (size_t)njobs; }
+
+extern "C" cudaError_t rs_setup_multi(const SetupJob* dJobs, const int* dChunk0, int njobs, int totalChunks, int maxPx,
+                                      int* counts, int* work, cudaStream_t s) {
+  if (njobs < 1) return cudaSuccess;
+  int* cntT = work;
+  int* cntC = work + totalChunks;
+  int* offT = work + 2 * (size_t)totalChunks;
+  int* offC = work + 3 * (size_t)totalChunks + njobs;
+  cudaMemsetAsync(counts, 0, 4 * (size_t)njobs * sizeof(int), s);
+  const int bx = std::max(1, std::min(blocks_for(maxPx, 256), 256));
+  k_setup_pixels<<<dim3(bx, njobs), 256, 0, s>>>(dJobs, counts);
+  k_setup_count<<<totalChunks, kThreads, 0, s>>>(dJobs, dChunk0, njobs, cntT, cntC);
+  k_setup_scan<<<njobs, kThreads, 0, s>>>(dChunk0, cntT, cntC, offT, offC, counts);
+  k_setup_compact<<<totalChunks, kThreads, 0, s>>>(dJobs, dChunk0, njobs, offT, offC);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t rs_writeback_multi(const SetupJob* dJobs, int njobs, int maxPx, cudaStream_t s) {
+  if (njobs < 1) return cudaSuccess;
+  const int bx = std::max(1, std::min(blocks_for(maxPx, 256), 256));
+  k_writeback<<<dim3(bx, njobs), 256, 0, s>>>(dJobs);
+  return cudaGetLastError();
+}
