@@ -1763,7 +1763,7 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
   CK(cudaEventRecord(e1, s));
   CK(cudaStreamSynchronize(s));
   for (size_t i = 0; i < jobs.size(); i++)
-    if (jobs[i].dCounts) {
+    if (jobs[i].setupIdx >= 0) {
       stats.evals += hostCtr[i].evals;
       stats.terms += hostCtr[i].terms;
     }
