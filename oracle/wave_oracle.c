@@ -382,7 +382,7 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
     /* corpus staged in shared memory when it fits: then probes stay per pixel */
     const size_t padWords = (((size_t)(cw + 12) * (ch + 12)) + 3) & ~(size_t)3;
     const size_t smem = 2064 + padWords * 4 * (w.nm ? 2 : 1) + 16 * 2048;
-    w.probeShare = opt->probeShare == 1 ? 1 : opt->probeShare == 2 ? 0 : (smem > WO_STAGED_LIMIT && n >= 131072) ? 1 : 0;
+    w.probeShare = opt->probeShare == 1 ? 1 : opt->probeShare == 2 ? 0 : smem > WO_STAGED_LIMIT ? 1 : 0;
     const int minPasses = opt->minPasses ? (int)opt->minPasses : ((!context && w.nm == 0) ? 3 : 0);
     unsigned ends[WO_PASSES];
     {
@@ -426,7 +426,8 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
          * context (wave_first_band in synth_host.cpp) */
         const unsigned firstRandom = context && (unsigned)n / 1024u > 16u ? (unsigned)n / 1024u : 16u;
         const double first = opt->firstBatch ? opt->firstBatch : (randomOrder ? (double)firstRandom : 1024.0);
-        const double growth = (opt->bandGrowth ? opt->bandGrowth : 200u) / 100.0;
+        /* bands double, or quadruple with map channels (wave_band_growth) */
+        const double growth = (opt->bandGrowth ? opt->bandGrowth : (w.nm ? 400u : 200u)) / 100.0;
         double size = randomOrder ? first : fmax(first, ceil((double)end / WO_MAX_BANDS)), b = 0;
         while (b < end && nb < WO_MAX_BANDS - 1) {
           b = fmin((double)end, b + fmax(1.0, size));

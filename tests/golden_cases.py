@@ -61,7 +61,7 @@ def frozen():
 WAVE_FULL = {
     "render1024": ("710baea67bc0c8500ffee84cb1251b01baeb669d22987efcde6304f5d6489edd", 3, [1048576, 51668, 23402]),
     "heal4096": ("6339cdc79ad835d4363eb096c3facba71d2cc81fc663fc10540c6c1cd4146d65", 2, [1523352, 59388]),
-    "mapstyle2048": ("45f09923a9f0f492c256d8752cf9eecb04ee2ff39533f0a7cd86c43d4a104091", 2, [4194304, 71126]),
+    "mapstyle2048": ("289dc9dd0a88eb8e04c691afe903695b2818f3472e1c91282c3eaacfc072eaf4", 2, [4194304, 71676]),
 }
 
 
@@ -87,7 +87,7 @@ WAVE_SMALL = {
     "heal": ("c242d24b4fd897e0f3b05f1f20d2c53a1b2334934f660664a5eb2ae4230e2eed", 3, [196, 39, 5]),
     "render": ("ab1318035955c00230beda01b7983e6105570027b8bdc5d8e9dc027a666a06ef", 3, [4096, 558, 217]),
     "render_tiled": ("3fedb93d5756a96d6ca9558a2285e458ab9a3cd3d148a05d755a976f38c985a0", 3, [4096, 762, 313]),
-    "mapstyle": ("784df1c59b1ed927bf680c27d91aeea78723242469524e590d968b3a0786da33", 2, [4096, 315]),
+    "mapstyle": ("53045f164606779ffc8d67ff21b240a025e9e2b1e80ae75538d6581e8fdad6e9", 2, [4096, 292]),
 }
 
 
