@@ -333,12 +333,12 @@ def learned_comparison(size, train_images, train_pairs, train_steps, searches, r
     from resynthesizer_gb300 import workloads as W
     fmt = R.format_indices(3, 0, 0, 0, 0)
 
-    def run(wl, trys, net=None, dump=None, stride=16, state=True):
+    def run(wl, trys, net=None, dump=None, stride=16, state=True, passes=0):
         tgt, cor = W.simple_to_pixmaps(wl["image"], wl["mask"])
         kw = dict(wl["params"])
         kw["maxProbeCount"] = trys
         o = R.options(mode=R.MODE_WAVEFRONT, recordState=1 if state else 0, net=net, proposals=16 if net else 0,
-                      dump=dump, dumpStride=stride)
+                      dump=dump, dumpStride=stride, proposalPasses=passes)
         r = R.engine(tgt, cor, fmt, R.params(**kw), opts=o)
         assert r.rc == 0, R.last_error()
         e = None
@@ -363,12 +363,15 @@ def learned_comparison(size, train_images, train_pairs, train_steps, searches, r
     train_s = time.perf_counter() - t0
     wl = W.heal4096(index=0, size=size)
     rows = []
-    for trys, use in searches:
+    for search in searches:
+        trys, use = search[0], search[1]
+        passes = search[2] if len(search) > 2 else 0
         ms = []
         for _ in range(reps):
-            r, e = run(wl, trys, net=net if use else None)
+            r, e = run(wl, trys, net=net if use else None, passes=passes)
             ms.append(r.stats["deviceMs"])
-        rows.append({"search": ("learned+" if use else "plain ") + f"trys={trys}", "energy": e,
+        rows.append({"search": ("learned+" if use else "plain ") + f"trys={trys}" +
+                               (f" (proposals in pass 0 only)" if passes == 1 else ""), "energy": e,
                      "ms": min(ms), "px_per_s": wl["target_px"] / (min(ms) / 1000.0), "evals": r.stats["evals"],
                      "passes": r.stats["passes"]})
     base = rows[0]["energy"]
@@ -871,7 +874,8 @@ def main():
                 try:
                     extra["learned_heal4096"] = learned_comparison(4096, 64, 2000000, 4000,
                                                                    [(200, False), (64, False), (16, False),
-                                                                    (200, True), (64, True), (16, True)], reps=2,
+                                                                    (200, True), (64, True), (16, True),
+                                                                    (64, True, 1), (16, True, 1)], reps=2,
                                                                    pool=pool)
                 except Exception as e:
                     extra["learned_heal4096"] = {"error": repr(e)[:300]}

@@ -164,8 +164,10 @@ typedef struct {
   unsigned int bandGrowthLarge; /* wavefront: growth in percent of pass-0 bands of at least 1/64 of the pass (0 = default) */
   int batchLaunches;          /* wavefront: how passes are launched (the output is the same): 0 = chosen per
                                  problem class across calls (persistent cooperative launches with grid barriers
-                                 between batches, 16 or 8 warps per CTA, or one launch per batch: the fastest of
-                                 the first three calls of the class); 1 = one launch per batch; 2 = persistent */
+                                 between batches, 16 or 8 warps per CTA, or one launch per batch: the fastest
+                                 over the first six calls of the class); 1 = one launch per batch; 2 = persistent */
+  unsigned int proposalPasses; /* wavefront with a network: score its proposals in the first proposalPasses passes
+                                 only (0 = every pass) */
 } TResynthOptions;
 
 typedef struct {

@@ -1144,6 +1144,9 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
         wa.pb.cellsH = cellsH;
       }
       const int nbatches = nb * k * k;
+      // the network's proposals in every pass, or in the first proposalPasses
+      const bool netPass = net && (!opt.proposalPasses || pass < (int)opt.proposalPasses);
+      if (!netPass) wa.props = nullptr;
       wa.pass = (unsigned)pass;
       wa.sparse = (pass == 0 && sparseOk) ? 1 : 0;
       const bool tuning = autoWarps && pass == 1 && nbatches >= 3;
@@ -1169,7 +1172,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
           maxCtas = expect < 1 << 20 ? (int)expect : 0;
           maxCommit = (int)std::min<long long>(1 << 20, expect / 256 + 1);
         }
-        if (net && b % (k * k) == 0) {
+        if (netPass && b % (k * k) == 0) {
           const int band = b / (k * k);
           const int count = bandEnds[band] - (band ? bandEnds[band - 1] : 0);
           CK(rs_net_propose(net, wa.pb, dPass, batchStart, b, b + k * k, count, pass == 0 ? b : 0x7ffffffe, props,
