@@ -388,7 +388,57 @@ def learned_comparison(size, train_images, train_pairs, train_steps, searches, r
             "learned_vs_plain_px_per_s_at_equal_energy": (best["px_per_s"] / rows[0]["px_per_s"]) if best else None}
 
 
-def run_learned(args):
+def learned_mapstyle(out=1024, train_images=8, steps=1000, reps=2):
+    """Map-conditioned proposals on the map-guided family (a 512^2 corpus
+    with its blurred-luma map -> an out^2 target guided by a smooth map, map
+    weight 0.5, P=30): pairs from plain runs over `train_images` problems
+    (seeds 1..N; the contexts carry the target map's first channel), the
+    network trained on the GPU, then the held-out problem (seed 0) with and
+    without its 16 proposals."""
+    import numpy as np
+
+    import resynthesizer_gb300 as R
+    from resynthesizer_gb300 import workloads as W
+
+    def run(wl, trys, net=None, dump=None):
+        kw = dict(wl["params"], maxProbeCount=trys)
+        fmt = R.format_indices(*wl["format"])
+        r = R.engine(wl["target"], wl["corpus"], fmt, R.params(**kw),
+                     opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1, net=net, proposals=16 if net else 0,
+                                    dump=dump, dumpStride=4))
+        assert r.rc == 0, R.last_error()
+        ys, xs = np.nonzero(wl["target"][..., 0] != 0)
+        t = np.stack([xs, ys], 1).astype(np.int32)
+        e, _ = R.patch_energy(R.params(**kw), fmt, r.out, wl["corpus"], r.has_value, r.source, t)
+        return r, e
+
+    pairs = R.Pairs(2000000)
+    for i in range(1, train_images + 1):
+        run(W.mapstyle(512, out, index=i), 200, dump=pairs)
+    net = R.Net(seed=1)
+    t0 = time.perf_counter()
+    loss = net.train(pairs, steps=steps, batch=512, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    wl = W.mapstyle(512, out, index=0)
+    rows = []
+    for trys, use in ((200, False), (64, False), (200, True), (64, True)):
+        ms = []
+        for _ in range(reps):
+            r, e = run(wl, trys, net=net if use else None)
+            ms.append(r.stats["deviceMs"])
+        rows.append({"search": ("learned+" if use else "plain ") + f"trys={trys}", "energy": e, "ms": min(ms),
+                     "px_per_s": out * out / (min(ms) / 1000.0)})
+    for row in rows:
+        row["energy_vs_plain200"] = row["energy"] / rows[0]["energy"]
+    npairs = len(pairs)
+    net.close()
+    pairs.close()
+    return {"learned": f"mapstyle{out}: 512^2 corpus + map, map weight 0.5, P=30, map channel in the context",
+            "train_problems": train_images, "train_pairs": npairs, "train_steps": steps, "train_s": train_s,
+            "train_loss": loss, "rows": rows}
+
+
+def run_learned(args):def run_learned(args):
     """The full learned-vs-plain table (see learned_comparison)."""
     line = learned_comparison(args.learned_size, args.train_images, args.train_pairs, args.train_steps,
                               [(200, False), (64, False), (16, False), (200, True), (64, True), (16, True),
@@ -879,6 +929,10 @@ def main():
                                                                    pool=pool)
                 except Exception as e:
                     extra["learned_heal4096"] = {"error": repr(e)[:300]}
+                try:
+                    extra["learned_mapstyle1024"] = learned_mapstyle()
+                except Exception as e:
+                    extra["learned_mapstyle1024"] = {"error": repr(e)[:300]}
         line["workloads"] = extra
     print(json.dumps(line), flush=True)
 

@@ -166,6 +166,42 @@ def test_dump_pairs_match_final_state():
     pairs.close()
 
 
+def test_map_guided_proposals():
+    """Map-conditioned proposals (the survey's map-guided style transfer): the
+    dumped contexts carry the target map's first channel where the reference
+    would see it, a network trained on them proposes sources for a map-guided
+    synthesis, and that synthesis keeps every invariant and is deterministic."""
+    wl = W.mapstyle(corpus_size=48, out=96, index=3)
+    tgt, cor, kw = wl["target"], wl["corpus"], wl["params"]
+    fmt = R.format_indices(*wl["format"])
+    pairs = R.Pairs(100000)
+    r = R.engine(tgt, cor, fmt, R.params(**kw),
+                 opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1, dump=pairs, dumpStride=5))
+    assert r.rc == 0
+    ys, xs = np.nonzero(tgt[..., 0] != 0)
+    pos = np.stack([xs, ys], 1)[::5]
+    x, lab = pairs.read()
+    assert len(x) == len(pos)
+    mapc = tgt[..., fmt.map_start_bip]
+    colors = r.out[..., 1:1 + fmt.img_match_bpp]
+    for i in range(1, len(pos), 2):                # complete contexts: the final image and the map
+        tx, ty = pos[i]
+        assert np.array_equal(x[i], N.context(colors, r.has_value.astype(bool), mapc, tx, ty)), i
+    net = R.Net(seed=4)
+    net.train(pairs, steps=300, batch=256, lr=1e-3)
+    runs = [R.engine(tgt, cor, fmt, R.params(**kw),
+                     opts=R.options(mode=R.MODE_WAVEFRONT, recordState=1, net=net, proposals=16)) for _ in range(2)]
+    assert all(q.rc == 0 for q in runs) and np.array_equal(runs[0].out, runs[1].out)
+    q = runs[0]
+    sel = tgt[..., 0] != 0
+    src = q.source[sel]
+    assert (src[:, 0] >= 0).all()
+    assert (q.out[sel][:, 1:4] == cor[src[:, 1], src[:, 0], 1:4]).all()
+    assert (q.out[..., fmt.map_start_bip] == tgt[..., fmt.map_start_bip]).all()
+    net.close()
+    pairs.close()
+
+
 def _heal_run(wl, net=None, proposals=0, trys=None):
     tgt, cor = W.simple_to_pixmaps(wl["image"], wl["mask"])
     kw = dict(wl["params"])
