@@ -438,7 +438,7 @@ def learned_mapstyle(out=1024, train_images=8, steps=1000, reps=2):
             "train_loss": loss, "rows": rows}
 
 
-def run_learned(args):def run_learned(args):
+def run_learned(args):
     """The full learned-vs-plain table (see learned_comparison)."""
     line = learned_comparison(args.learned_size, args.train_images, args.train_pairs, args.train_steps,
                               [(200, False), (64, False), (16, False), (200, True), (64, True), (16, True),
