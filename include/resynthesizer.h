@@ -168,6 +168,9 @@ typedef struct {
                                  over the first six calls of the class); 1 = one launch per batch; 2 = persistent */
   unsigned int proposalPasses; /* wavefront with a network: score its proposals in the first proposalPasses passes
                                  only (0 = every pass) */
+  int probeShare;             /* wavefront: random probes keyed per target pixel or shared by groups of 16 batch
+                                 slots: 0 = shared when the corpus is read from global memory, 1 = always
+                                 shared, 2 = never */
 } TResynthOptions;
 
 typedef struct {

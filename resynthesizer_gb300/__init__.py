@@ -61,7 +61,7 @@ class Options(C.Structure):
                 ("phaseSide", C.c_uint), ("bandGrowth", C.c_uint), ("minPasses", C.c_uint),
                 ("net", C.c_void_p), ("proposals", C.c_uint), ("dumpPairs", C.c_void_p), ("dumpStride", C.c_uint),
                 ("graphs", C.c_int), ("separateRequests", C.c_int), ("bandGrowthLarge", C.c_uint),
-                ("batchLaunches", C.c_int), ("proposalPasses", C.c_uint)]
+                ("batchLaunches", C.c_int), ("proposalPasses", C.c_uint), ("probeShare", C.c_int)]
 
 
 class TrainOptions(C.Structure):
@@ -185,7 +185,7 @@ def format_indices(colors, mapColors=0, alphaTarget=0, alphaSource=0, isMap=0) -
 def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, recordState=0,
             profile=0, phaseSide=0, bandGrowth=0, minPasses=0, net=None, proposals=0, dump=None,
             dumpStride=0, graphs=0, separateRequests=0, bandGrowthLarge=0, batchLaunches=0,
-            proposalPasses=0) -> Options:
+            proposalPasses=0, probeShare=0) -> Options:
     o = Options()
     lib().resynthDefaultOptions(C.byref(o))
     if mode is not None:
@@ -201,6 +201,7 @@ def options(mode=None, seed=0, firstBatch=0, refineBatches=0, warpsPerBlock=0, r
     o.separateRequests = separateRequests
     o.batchLaunches = batchLaunches
     o.proposalPasses = proposalPasses
+    o.probeShare = probeShare
     o.bandGrowthLarge = bandGrowthLarge
     return o
 

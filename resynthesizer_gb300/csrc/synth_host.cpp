@@ -1084,7 +1084,7 @@ int run_engine_device(const TImageSynthParameters& p, const TFormatIndices& f, u
     // (heal 512^2 and 1024^2, render 256^2 and 512^2, map-guided 512^2; four
     // seeds each).  Problems whose corpus sits in shared memory keep
     // per-pixel probes.
-    wa.probeShare = rs_wave_corpus_staged(dp.pb, 16) ? 0 : 1;
+    wa.probeShare = opt.probeShare == 1 ? 1 : opt.probeShare == 2 ? 0 : rs_wave_corpus_staged(dp.pb, 16) ? 0 : 1;
     const bool autoWarps = opt.warpsPerBlock == 0 && warps == 0;
     if (!warps) warps = 16;
     static const int kTryWarps[3] = {16, 8, 4};
@@ -1578,7 +1578,7 @@ int run_batch_wave(std::vector<TResynthRequest*>& reqs, const TResynthOptions& o
     wa.stageSrc = ar.alloc<int2>(J.ntargets);
     wa.targets = J.dPass;
     wa.batchStart = J.batchStart;
-    wa.probeShare = rs_wave_corpus_staged(pb, 16) ? 0 : 1;
+    wa.probeShare = opt.probeShare == 1 ? 1 : opt.probeShare == 2 ? 0 : rs_wave_corpus_staged(pb, 16) ? 0 : 1;
     J.active = true;
   }
   // 3. passes
