@@ -243,6 +243,36 @@ static int phase_side(const wpt *offs, int noffs, int limit, int w, int h) {
   return k;
 }
 
+/* The wavefront offset list: every offset within 256 px in ascending
+ * dx^2 + dy^2, ties by descending position in the box (descending dy, then
+ * descending dx) -- an order that does not depend on the box; each call cuts
+ * it at min(box diagonal, 256)^2.  Built once per process. */
+static pthread_once_t g_offs_once = PTHREAD_ONCE_INIT;
+static wpt *g_offs_all;
+static size_t g_noffs_all;
+
+static void build_offsets(void) {
+  const int W = 2 * 257 - 1;
+  uint64_t *keys = malloc((size_t)W * W * sizeof *keys);
+  size_t nall = 0;
+  for (int y = -256; y <= 256; y++)
+    for (int x = -256; x <= 256; x++) {
+      const long long d2 = (long long)x * x + (long long)y * y;
+      if (d2 > 65536) continue;
+      const uint32_t idx = (uint32_t)((y + 256) * W + (x + 256));
+      keys[nall++] = ((uint64_t)d2 << 32) | (uint32_t)~idx;
+    }
+  qsort(keys, nall, sizeof *keys, cmp_u64);
+  g_offs_all = malloc(nall * sizeof *g_offs_all);
+  for (size_t i = 0; i < nall; i++) {
+    const uint32_t idx = ~(uint32_t)(keys[i] & 0xffffffffu);
+    g_offs_all[i].x = (int)(idx % W) - 256;
+    g_offs_all[i].y = (int)(idx / W) - 256;
+  }
+  g_noffs_all = nall;
+  free(keys);
+}
+
 /* The wavefront engine on interleaved pixmaps (the GPU library's engine()
  * in its default mode), random orders only.  target is modified in place
  * (colours).  Returns 0, or -1 for an unsupported order.  passesOut and
@@ -350,32 +380,16 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
     goto done;
   }
   {
-    /* the wavefront offset list: every offset within 256 px in ascending
-     * dx^2 + dy^2, ties by descending position in the box (descending dy,
-     * then descending dx) -- an order that does not depend on the box --
-     * cut at min(box diagonal, 256)^2 */
-    const int W = 2 * 257 - 1;
-    uint64_t *keys = malloc((size_t)W * W * sizeof *keys);
-    size_t nall = 0;
+    /* the shared offset list (build_offsets), cut at min(box diagonal, 256)^2 */
+    pthread_once(&g_offs_once, build_offsets);
     long long full = (long long)(w.boxW - 1) * (w.boxW - 1) + (long long)(w.boxH - 1) * (w.boxH - 1);
     const long long maxD2 = full < 65536 ? full : 65536;
-    for (int y = -256; y <= 256; y++)
-      for (int x = -256; x <= 256; x++) {
-        const long long d2 = (long long)x * x + (long long)y * y;
-        if (d2 > 65536) continue;
-        const uint32_t idx = (uint32_t)((y + 256) * W + (x + 256));
-        keys[nall++] = ((uint64_t)d2 << 32) | (uint32_t)~idx;
-      }
-    qsort(keys, nall, sizeof *keys, cmp_u64);
-    wpt *offs = malloc(nall * sizeof *offs);
+    const size_t nall = g_noffs_all;
+    const wpt *offs = g_offs_all;
     int noffs = 0;
-    for (size_t i = 0; i < nall; i++) {
-      const uint32_t idx = ~(uint32_t)(keys[i] & 0xffffffffu);
-      offs[i].x = (int)(idx % W) - 256;
-      offs[i].y = (int)(idx / W) - 256;
-      if ((long long)(keys[i] >> 32) <= maxD2) noffs = (int)i + 1;
-    }
-    free(keys);
+    while ((size_t)noffs < nall &&
+           (long long)offs[noffs].x * offs[noffs].x + (long long)offs[noffs].y * offs[noffs].y <= maxD2)
+      noffs++;
     w.offs = offs;
     w.noffs = noffs;
     const int k = opt->phaseSide ? (int)opt->phaseSide : phase_side(offs, (int)nall, w.limit, w.boxW, w.boxH);
@@ -405,7 +419,6 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
     } else {
       if (orc_order_targets(p->matchContextType, (orc_pt *)targets, (unsigned)n)) {
         free(rank);
-        free(offs);
         rc = -1;
         goto done;
       }
@@ -496,7 +509,6 @@ int orc_wave_engine_ex(const orc_params *p, const orc_format *f, unsigned char *
     free(bucket);
     free(start);
     free(w.stage);
-    free(offs);
   }
   /* colours back into the pixmap */
   for (size_t i = 0; i < tn; i++)

@@ -175,3 +175,28 @@ def test_wavefront_edge_cases_vs_oracle(oracle, case):
     s = R.image_synth(img, mask, fmt, R.params(**kw), opts=R.options(**WAVE))
     rc_o, out_o = oracle.wave_image_synth(img, mask, fmt, make_params(**kw))
     assert s.rc == rc_o == 0 and np.array_equal(s.out, out_o)
+
+
+def test_batch_more_requests_than_one_launch_takes(oracle):
+    """More requests than one persistent many-request launch takes (4096):
+    the pass is split into launches of at most 4096 requests.  4,300 tiny
+    heals of mixed layouts, each byte-identical to the restatement."""
+    rng = np.random.default_rng(41)
+    items = []
+    for i in range(4300):
+        fmt = [W.T_Gray, W.T_RGB, W.T_RGBA][i % 3]
+        h, w = int(rng.integers(6, 14)), int(rng.integers(6, 14))
+        img = rng.integers(0, 256, (h, w, W.PIXELELS[fmt]), dtype=np.uint8)
+        if fmt == W.T_RGBA:
+            img[..., 3] = 255
+        mask = np.zeros((h, w), np.uint8)
+        y0, x0 = int(rng.integers(1, h - 3)), int(rng.integers(1, w - 3))
+        mask[y0:y0 + 2, x0:x0 + 3] = 255
+        kw = dict(matchContextType=1, patchSize=[9, 16, 30][i % 3], maxProbeCount=20)
+        items.append((img, mask, fmt, kw))
+    rc, outs, codes, st = R.image_synth_batch([(a, b, c, R.params(**d)) for a, b, c, d in items],
+                                              opts=R.options(**WAVE), concurrency=4)
+    assert rc == 0 and codes == [0] * len(items), R.last_error()
+    for i, ((img, mask, fmt, kw), out) in enumerate(zip(items, outs)):
+        rc_o, out_o = oracle.wave_image_synth(img, mask, fmt, make_params(**kw), threads=1)
+        assert rc_o == 0 and np.array_equal(out, out_o), i
