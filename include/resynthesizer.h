@@ -286,8 +286,10 @@ int resynthOrderTargets(int matchContextType, const Coordinates *points, unsigne
  *   - All calls share the one working array: calls that may overlap on the GPU
  *     (on different streams without ordering between them) race and corrupt
  *     each other's results.  Every call rewrites everything it reads there.
- *   - The first call on each device looks up the array's device address with
- *     that device current; make that first call before any stream capture. */
+ *   - The call enqueues kernels only (the metric tables travel as kernel
+ *     arguments), so it can be captured into a CUDA graph; but the first
+ *     call on each device looks up the array's device address with that
+ *     device current, so make that first call before any stream capture. */
 int resynthFrozenBestFitNoAlloc(const TImageSynthParameters *parameters, const TFormatIndices *indices,
                                 const unsigned char *dTarget, unsigned int targetWidth, unsigned int targetHeight,
                                 const unsigned char *dCorpus, unsigned int corpusWidth, unsigned int corpusHeight,

@@ -20,6 +20,7 @@
 #include <climits>
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 #include <map>
 #include <mutex>
 
@@ -2005,6 +2006,15 @@ extern "C" void rs_metric_tables(double sensitivity, double mapWeight, uint32_t*
 namespace rs {
 namespace {
 
+// One metric table as a kernel argument (2 KiB of parameter space): the
+// launch carries the values, which a captured graph keeps with the node.
+struct TableArg {
+  uint32_t v[kTable];
+};
+__global__ void __launch_bounds__(256) k_store_table(TableArg t, uint32_t* dst) {
+  for (int i = threadIdx.x; i < kTable; i += blockDim.x) dst[i] = t.v[i];
+}
+
 constexpr size_t kNoAllocScratchBytes = 8u << 20;   // 8 MiB
 constexpr size_t kNoAllocTableBytes = 2 * kTable * sizeof(uint32_t);
 static __device__ __align__(256) unsigned char g_noAllocScratch[kNoAllocScratchBytes];
@@ -2242,7 +2252,14 @@ extern "C" __attribute__((visibility("default"))) int resynthFrozenBestFitNoAllo
   uint32_t* tmap = maps ? tpx + tWords : nullptr;
   uint32_t* cpx = tpx + tWords * (maps ? 2 : 1);
   uint32_t* cmap = maps ? cpx + cWords : nullptr;
-  e = cudaMemcpyAsync(dTables, tables, sizeof tables, cudaMemcpyHostToDevice, s);
+  // the tables travel as kernel arguments: no host copy is enqueued, so a
+  // call after the first on a device can be captured into a CUDA graph
+  for (int t = 0; t < 2; t++) {
+    TableArg arg;
+    memcpy(arg.v, tables + t * kTable, sizeof arg.v);
+    k_store_table<<<1, 256, 0, s>>>(arg, dTables + t * kTable);
+  }
+  e = cudaGetLastError();
   if (e == cudaSuccess)
     e = rs_launch_pack(dTarget, (int)tw, (int)th, f->total_bpp, 1, f->img_match_bpp, f->map_start_bip,
                        f->map_match_bpp, tpx, tmap, s);

@@ -123,3 +123,42 @@ def test_no_alloc_rejects_oversized_images(lib):
                                          C.c_void_p(1), C.c_void_p(1), C.c_void_p(1), 0, C.c_void_p(1),
                                          C.c_void_p(1), C.c_void_p(1), C.c_void_p(1), C.c_void_p(1), None)
     assert rc == 101 and "8 MiB" in R.last_error()
+
+
+def test_no_alloc_call_captured_in_graph(lib):
+    # After the first call on a device, a call enqueues kernels only (the
+    # metric tables travel as kernel arguments), so it can be captured into a
+    # CUDA graph.  Another problem with other metric parameters runs between
+    # capture and replay: the replay rewrites the whole working array itself.
+    import torch
+    dev = torch.device("cuda", 0)
+    prob = _problem(606, (3, 1, 0, 0, 1), 70, 60, 80, 50, 0)
+    params, fmt, target, corpus, has, src, targets, start, cands = prob
+    params.sensitivityToOutliers = 0.3
+    want = _no_alloc(lib, *prob)
+    other = _problem(707, (3, 0, 0, 0, 0), 50, 40, 60, 30, 1)
+    other[0].sensitivityToOutliers = 0.05
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+         for k, v in dict(target=target, corpus=corpus, has=has, src=src, targets=targets,
+                          start=start.view(np.int32), cands=cands).items()}
+    n = len(targets)
+    outs = [torch.zeros(n, dtype=torch.int32, device=dev), torch.zeros((n, 2), dtype=torch.int32, device=dev),
+            torch.zeros(n, dtype=torch.int32, device=dev)]
+    th, tw, _ = target.shape
+    ch, cw, _ = corpus.shape
+    vp = C.c_void_p
+    torch.cuda.synchronize(dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = lib.resynthFrozenBestFitNoAlloc(
+            C.byref(params), C.byref(fmt), vp(t["target"].data_ptr()), tw, th, vp(t["corpus"].data_ptr()), cw, ch,
+            vp(t["has"].data_ptr()), vp(t["src"].data_ptr()), vp(t["targets"].data_ptr()), n,
+            vp(t["start"].data_ptr()), vp(t["cands"].data_ptr()), vp(outs[0].data_ptr()), vp(outs[1].data_ptr()),
+            vp(outs[2].data_ptr()), vp(torch.cuda.current_stream(dev).cuda_stream))
+    assert rc == 0, R.last_error()
+    _no_alloc(lib, *other)
+    g.replay()
+    torch.cuda.synchronize(dev)
+    got = (outs[0].cpu().numpy().view(np.uint32), outs[1].cpu().numpy(), outs[2].cpu().numpy().view(np.uint32))
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
