@@ -156,29 +156,41 @@ __device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int
   return count;
 }
 
-// Inserts one key per lane into the warp's ascending list best[0 .. cnt)
-// holding the lim smallest keys seen; thr = the lim-th key once full.
-__device__ __forceinline__ void topk_insert(unsigned long long key, unsigned long long* best, int& cnt,
-                                            unsigned long long& thr, int lim, int lane) {
-  unsigned m = __ballot_sync(kFull, key < thr);
-  while (m) {
-    const int srcLane = __ffs(m) - 1;
-    m &= m - 1;
-    const unsigned long long k = __shfl_sync(kFull, key, srcLane);
-    if (k >= thr) continue;
-    const unsigned long long e0 = lane < cnt ? best[lane] : ~0ull;
-    const unsigned long long e1 = lane + 32 < cnt ? best[lane + 32] : ~0ull;
-    const int pos = __popc(__ballot_sync(kFull, e0 < k)) + __popc(__ballot_sync(kFull, e1 < k));
-    __syncwarp();
-    if (lane >= pos && lane < cnt && lane + 1 < lim) best[lane + 1] = e0;
-    if (lane + 32 >= pos && lane + 32 < cnt && lane + 33 < lim) best[lane + 33] = e1;
-    __syncwarp();
-    if (lane == 0) best[pos] = k;
-    __syncwarp();
-    cnt = min(cnt + 1, lim);
-    thr = cnt == lim ? best[lim - 1] : ~0ull;
+// The lim (<= 64) smallest keys a warp has seen, ascending, in registers:
+// lane i holds entries i (lo) and 32 + i (hi), entries from cnt on are ~0;
+// thr is the lim-th smallest once the list is full (else ~0).  An insertion
+// is a few shuffles and two votes, with no shared-memory round trip.
+struct WarpTopK {
+  unsigned long long lo = ~0ull, hi = ~0ull, thr = ~0ull;
+  int cnt = 0;
+  // Inserts the key each lane holds (~0: none).
+  __device__ __forceinline__ void insert(unsigned long long key, int lim, int lane) {
+    unsigned m = __ballot_sync(kFull, key < thr);
+    while (m) {
+      const int srcLane = __ffs(m) - 1;
+      m &= m - 1;
+      const unsigned long long k = __shfl_sync(kFull, key, srcLane);
+      if (k >= thr) continue;
+      const unsigned long long loUp = __shfl_up_sync(kFull, lo, 1), hiUp = __shfl_up_sync(kFull, hi, 1);
+      const unsigned long long lo31 = __shfl_sync(kFull, lo, 31);
+      const int pos = __popc(__ballot_sync(kFull, lo < k)) + __popc(__ballot_sync(kFull, hi < k));
+      // entry e moves to e + 1 from pos on; k takes entry pos; entries past lim drop
+      if (lane > pos) lo = loUp;
+      else if (lane == pos) lo = k;
+      if (32 + lane > pos) hi = lane == 0 ? lo31 : hiUp;
+      else if (32 + lane == pos) hi = k;
+      if (lane >= lim) lo = ~0ull;
+      if (32 + lane >= lim) hi = ~0ull;
+      cnt = min(cnt + 1, lim);
+      if (cnt == lim) thr = __shfl_sync(kFull, lim <= 32 ? lo : hi, (lim - 1) & 31);
+    }
   }
-}
+  // Writes the list to best[0 .. cnt).
+  __device__ __forceinline__ void store(unsigned long long* best, int lane) const {
+    if (lane < cnt) best[lane] = lo;
+    if (32 + lane < cnt) best[32 + lane] = hi;
+  }
+};
 
 // Sort key of neighbour offset (dx, dy): the sorted offset list's order,
 // ascending dx^2 + dy^2 with ties by descending position in the offset box.
@@ -188,28 +200,27 @@ __device__ __forceinline__ unsigned long long offset_key(const Problem& pb, int 
   return ((unsigned long long)((long long)dx * dx + (long long)dy * dy) << 32) | (0xFFFFFFFFu - idx);
 }
 
-// The patch from a finished key list: self, then the listed neighbours.
-__device__ int patch_from_keys(const Problem& pb, int px, int py, Patch& P, const unsigned long long* best, int cnt,
-                               int lane) {
+// The patch from a finished register list: self, then the listed neighbours.
+__device__ int patch_from_topk(const Problem& pb, int px, int py, Patch& P, const WarpTopK& tk, int lane) {
   const int bw = pb.boxW, bh = pb.boxH;
   const unsigned W2 = 2u * bw - 1u;
   if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
-  for (int i = lane; i < cnt; i += 32) {
-    const unsigned idx = 0xFFFFFFFFu - (unsigned)(best[i] & 0xffffffffu);
-    const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
-    load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int i = 32 * h + lane;
+    if (i < tk.cnt) {
+      const unsigned idx = 0xFFFFFFFFu - (unsigned)((h ? tk.hi : tk.lo) & 0xffffffffu);
+      const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
+      load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
+    }
   }
   __syncwarp();
-  return 1 + cnt;
+  return 1 + tk.cnt;
 }
 
-// Merges other key lists into best (a list of the lim smallest keys).
-__device__ void merge_keys(unsigned long long* best, int& cnt, unsigned long long& thr, int lim,
-                           const unsigned long long* other, int ocnt, int lane) {
-  for (int base = 0; base < ocnt; base += 32) {
-    const unsigned long long k = base + lane < ocnt ? other[base + lane] : ~0ull;
-    topk_insert(k, best, cnt, thr, lim, lane);
-  }
+// Merges another warp's key list (ocnt keys in shared memory) into tk.
+__device__ void merge_keys(WarpTopK& tk, int lim, const unsigned long long* other, int ocnt, int lane) {
+  for (int base = 0; base < ocnt; base += 32) tk.insert(base + lane < ocnt ? other[base + lane] : ~0ull, lim, lane);
 }
 
 // Patch neighbours when the valued pixels are exactly list[0 .. V) and nothing
@@ -217,8 +228,8 @@ __device__ void merge_keys(unsigned long long* best, int& cnt, unsigned long lon
 // a sorted key list instead of walking the offset list.  Part `part` of
 // `parts` warps takes every parts-th run of 32 list entries; merging the
 // parts' lists gives the whole list's lim smallest keys.
-__device__ void sparse_keys(const Problem& pb, int px, int py, unsigned long long* best, int& cnt,
-                            unsigned long long& thr, const int2* list, int V, int lane, int part, int parts) {
+__device__ void sparse_keys(const Problem& pb, int px, int py, WarpTopK& tk, const int2* list, int V, int lane,
+                            int part, int parts) {
   constexpr int kU = 4;   // list loads per lane in flight
   const int lim = pb.patchLimit - 1;
   const int bw = pb.boxW, bh = pb.boxH;
@@ -238,7 +249,7 @@ __device__ void sparse_keys(const Problem& pb, int px, int py, unsigned long lon
       }
     }
 #pragma unroll
-    for (int u = 0; u < kU; u++) topk_insert(key[u], best, cnt, thr, lim, lane);
+    for (int u = 0; u < kU; u++) tk.insert(key[u], lim, lane);
   }
 }
 
@@ -251,8 +262,8 @@ __device__ void sparse_keys(const Problem& pb, int px, int py, unsigned long lon
 // warps owns the cells whose ring index is congruent to it; each part stops
 // on its own bound, and merging the parts' lists gives the lim smallest keys
 // (a key among the lim smallest overall is among the lim smallest of its part).
-__device__ void grid_keys(const Problem& pb, int px, int py, unsigned long long* best, int& cnt,
-                          unsigned long long& thr, int lane, int visCur, int part, int parts) {
+__device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int lane, int visCur, int part,
+                          int parts) {
   const int lim = pb.patchLimit - 1;
   const int bw = pb.boxW, bh = pb.boxH;
   const int cx = px >> kCellShift, cy = py >> kCellShift;
@@ -262,7 +273,7 @@ __device__ void grid_keys(const Problem& pb, int px, int py, unsigned long long*
       // every pixel of ring R is at least (R - 1) * kCell + 1 away on one axis
       const long long dmin = (long long)(R - 1) * kCell + 1;
       if (dmin * dmin > pb.maxD2 || (dmin >= bw && dmin >= bh)) break;
-      if (cnt == lim && (unsigned long long)(dmin * dmin) > (thr >> 32)) break;
+      if (tk.cnt == lim && (unsigned long long)(dmin * dmin) > (tk.thr >> 32)) break;
     }
     const int ncell = R == 0 ? 1 : 8 * R;
     const int mine = ncell > part ? (ncell - part + parts - 1) / parts : 0;   // cells part, part + parts, ...
@@ -293,7 +304,7 @@ __device__ void grid_keys(const Problem& pb, int px, int py, unsigned long long*
           const int ddx = max(0, max(x0 - px, px - (x0 + kCell - 1)));
           const int ddy = max(0, max(y0 - py, py - (y0 + kCell - 1)));
           const long long d2 = (long long)ddx * ddx + (long long)ddy * ddy;
-          want = d2 <= pb.maxD2 && ddx < bw && ddy < bh && (cnt < lim || (unsigned long long)d2 <= (thr >> 32));
+          want = d2 <= pb.maxD2 && ddx < bw && ddy < bh && (tk.cnt < lim || (unsigned long long)d2 <= (tk.thr >> 32));
         }
       }
       unsigned wm = __ballot_sync(kFull, want);
@@ -323,19 +334,17 @@ __device__ void grid_keys(const Problem& pb, int px, int py, unsigned long long*
           }
         }
 #pragma unroll
-        for (int j = 0; j < kCell; j++) topk_insert(key[j], best, cnt, thr, lim, lane);
+        for (int j = 0; j < kCell; j++) tk.insert(key[j], lim, lane);
       }
     }
   }
 }
 
 // One warp: the whole grid search.
-__device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, unsigned long long* best, int lane,
-                                int visCur) {
-  int cnt = 0;
-  unsigned long long thr = ~0ull;
-  grid_keys(pb, px, py, best, cnt, thr, lane, visCur, 0, 1);
-  return patch_from_keys(pb, px, py, P, best, cnt, lane);
+__device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, int lane, int visCur) {
+  WarpTopK tk;
+  grid_keys(pb, px, py, tk, lane, visCur, 0, 1);
+  return patch_from_topk(pb, px, py, P, tk, lane);
 }
 
 // Offsets walked before a pass-0 patch falls back to the cell grid.
@@ -878,8 +887,7 @@ __device__ __forceinline__ unsigned wave_target(const WaveArgs& a, const Problem
   const int G = T.G, tw = T.tw, lead = T.lead, lane = T.lane, warp = T.warp;
   unsigned char* wbase = T.region(lead);
   Patch& P = *reinterpret_cast<Patch*>(wbase);
-  unsigned long long* topk = reinterpret_cast<unsigned long long*>(wbase + sizeof(Patch));
-  int2* prop = reinterpret_cast<int2*>(topk);
+  int2* prop = reinterpret_cast<int2*>(wbase + sizeof(Patch));   // continuation candidates
   const int t = b0 + slot;
   const int2 pos = a.targets[t];
   const int pi = pos.y * pb.tw + pos.x;
@@ -889,24 +897,24 @@ __device__ __forceinline__ unsigned wave_target(const WaveArgs& a, const Problem
   // the cell grid when the nearest values lie beyond the walk's reach.
   int nPatch = 0;
   if (sparse) {
-    unsigned long long* mine = reinterpret_cast<unsigned long long*>(T.region(warp) + sizeof(Patch));
-    int cnt = 0;
-    unsigned long long thr = ~0ull;
-    sparse_keys(pb, pos.x, pos.y, mine, cnt, thr, a.targets, b0, lane, tw, G);
+    WarpTopK tk;
+    sparse_keys(pb, pos.x, pos.y, tk, a.targets, b0, lane, tw, G);
     if (G > 1) {
-      if (lane == 0) T.sGather[warp] = cnt;
+      // the other warps' lists go through their top-list areas
+      if (tw > 0) tk.store(reinterpret_cast<unsigned long long*>(T.region(warp) + sizeof(Patch)), lane);
+      if (lane == 0) T.sGather[warp] = tk.cnt;
       T.sync();
       if (tw == 0)
         for (int w = 1; w < G; w++)
-          merge_keys(mine, cnt, thr, pb.patchLimit - 1,
+          merge_keys(tk, pb.patchLimit - 1,
                      reinterpret_cast<const unsigned long long*>(T.region(lead + w) + sizeof(Patch)),
                      T.sGather[lead + w], lane);
     }
-    if (tw == 0) nPatch = patch_from_keys(pb, pos.x, pos.y, P, mine, cnt, lane);
+    if (tw == 0) nPatch = patch_from_topk(pb, pos.x, pos.y, P, tk, lane);
   } else if (tw == 0) {
     nPatch = build_patch_warp(pb, pos.x, pos.y, P, lane, visCur, pb.cellMin ? kScanCap : INT_MAX);
     if (pb.cellMin && nPatch < pb.patchLimit && kScanCap < pb.noffs)
-      nPatch = build_patch_grid(pb, pos.x, pos.y, P, topk, lane, visCur);
+      nPatch = build_patch_grid(pb, pos.x, pos.y, P, lane, visCur);
   }
   if (tw == 0) {
     const int n = nPatch;
@@ -1672,11 +1680,10 @@ extern "C" cudaError_t rs_launch_energy(const ScoreArgs& a, cudaStream_t s) {
 __global__ void __launch_bounds__(256) k_patches(Problem pb, const int2* targets, int n, int visCur, int useGrid,
                                                  int* outOff, int* outCount) {
   __shared__ Patch sp[8];
-  __shared__ unsigned long long sk[8][kMaxNeighbors];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int t = blockIdx.x * 8 + w; t < n; t += gridDim.x * 8) {
     const int2 pos = targets[t];
-    const int cnt = useGrid ? build_patch_grid(pb, pos.x, pos.y, sp[w], sk[w], lane, visCur)
+    const int cnt = useGrid ? build_patch_grid(pb, pos.x, pos.y, sp[w], lane, visCur)
                             : build_patch_warp(pb, pos.x, pos.y, sp[w], lane, visCur);
     for (int i = 1 + lane; i < cnt; i += 32) outOff[(size_t)t * kMaxNeighbors + i - 1] = sp[w].off[i];
     if (lane == 0) outCount[t] = cnt - 1;
