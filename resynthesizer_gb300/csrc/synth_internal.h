@@ -37,7 +37,8 @@ struct Problem {
   int patchLimit;             // the patch stops growing at max(patchSize, 2) neighbours
   int tileH, tileV;
   int boxW, boxH;             // offsets span |dx| < boxW, |dy| < boxH (the smaller image)
-  long long maxD2;            // offsets are cut at dx^2 + dy^2 <= maxD2
+  long long maxD2;            // offsets are cut at dx^2 + dy^2 <= maxD2 (wavefront: at most 256^2, which the
+                              // pass-0 nearest-key lists pack into 32-bit keys)
   int fullCorpus;             // every corpus pixel is a corpus point: probes need no list
   uint32_t clipCost;          // 65535 * nc + mapTable[0] * nm
   const uint32_t* ctab;       // colour metric table (512 entries, widened to 32 bits)

@@ -157,61 +157,105 @@ __device__ int build_patch_warp(const Problem& pb, int px, int py, Patch& P, int
 }
 
 // The lim (<= 64) smallest keys a warp has seen, ascending, in registers:
-// lane i holds entries i (lo) and 32 + i (hi), entries from cnt on are ~0;
-// thr is the lim-th smallest once the list is full (else ~0).  An insertion
-// is a few shuffles and two votes, with no shared-memory round trip.
+// lane i holds entries i (lo) and 32 + i (hi), entries from cnt on are
+// kNoKey; thr is the lim-th smallest once the list is full (else kNoKey).
+// An insertion is a few shuffles and two votes, with no shared-memory round
+// trip.
+constexpr uint32_t kNoKey = 0xFFFFFFFFu;
 struct WarpTopK {
-  unsigned long long lo = ~0ull, hi = ~0ull, thr = ~0ull;
+  uint32_t lo = kNoKey, hi = kNoKey, thr = kNoKey;
   int cnt = 0;
-  // Inserts the key each lane holds (~0: none).
-  __device__ __forceinline__ void insert(unsigned long long key, int lim, int lane) {
+  // Inserts the key each lane holds (kNoKey: none).
+  __device__ __forceinline__ void insert(uint32_t key, int lim, int lane) {
     unsigned m = __ballot_sync(kFull, key < thr);
     while (m) {
       const int srcLane = __ffs(m) - 1;
       m &= m - 1;
-      const unsigned long long k = __shfl_sync(kFull, key, srcLane);
+      const uint32_t k = __shfl_sync(kFull, key, srcLane);
       if (k >= thr) continue;
-      const unsigned long long loUp = __shfl_up_sync(kFull, lo, 1), hiUp = __shfl_up_sync(kFull, hi, 1);
-      const unsigned long long lo31 = __shfl_sync(kFull, lo, 31);
+      const uint32_t loUp = __shfl_up_sync(kFull, lo, 1), hiUp = __shfl_up_sync(kFull, hi, 1);
+      const uint32_t lo31 = __shfl_sync(kFull, lo, 31);
       const int pos = __popc(__ballot_sync(kFull, lo < k)) + __popc(__ballot_sync(kFull, hi < k));
       // entry e moves to e + 1 from pos on; k takes entry pos; entries past lim drop
       if (lane > pos) lo = loUp;
       else if (lane == pos) lo = k;
       if (32 + lane > pos) hi = lane == 0 ? lo31 : hiUp;
       else if (32 + lane == pos) hi = k;
-      if (lane >= lim) lo = ~0ull;
-      if (32 + lane >= lim) hi = ~0ull;
+      if (lane >= lim) lo = kNoKey;
+      if (32 + lane >= lim) hi = kNoKey;
       cnt = min(cnt + 1, lim);
       if (cnt == lim) thr = __shfl_sync(kFull, lim <= 32 ? lo : hi, (lim - 1) & 31);
     }
   }
   // Writes the list to best[0 .. cnt).
-  __device__ __forceinline__ void store(unsigned long long* best, int lane) const {
+  __device__ __forceinline__ void store(uint32_t* best, int lane) const {
     if (lane < cnt) best[lane] = lo;
     if (32 + lane < cnt) best[32 + lane] = hi;
   }
 };
 
-// Sort key of neighbour offset (dx, dy): the sorted offset list's order,
-// ascending dx^2 + dy^2 with ties by descending position in the offset box.
-__device__ __forceinline__ unsigned long long offset_key(const Problem& pb, int dx, int dy) {
-  const unsigned W2 = 2u * pb.boxW - 1u;
-  const unsigned idx = (unsigned)(dy + pb.boxH - 1) * W2 + (unsigned)(dx + pb.boxW - 1);
-  return ((unsigned long long)((long long)dx * dx + (long long)dy * dy) << 32) | (0xFFFFFFFFu - idx);
+// Sorts four or eight keys of one lane ascending (comparator networks).
+__device__ __forceinline__ void cmp_swap(uint32_t& a, uint32_t& b) {
+  const uint32_t l = min(a, b);
+  b = max(a, b);
+  a = l;
+}
+__device__ __forceinline__ void sort4(uint32_t* v) {
+  cmp_swap(v[0], v[1]);
+  cmp_swap(v[2], v[3]);
+  cmp_swap(v[0], v[2]);
+  cmp_swap(v[1], v[3]);
+  cmp_swap(v[1], v[2]);
+}
+__device__ __forceinline__ void sort8(uint32_t* v) {
+  cmp_swap(v[0], v[2]);
+  cmp_swap(v[1], v[3]);
+  cmp_swap(v[4], v[6]);
+  cmp_swap(v[5], v[7]);
+  cmp_swap(v[0], v[4]);
+  cmp_swap(v[1], v[5]);
+  cmp_swap(v[2], v[6]);
+  cmp_swap(v[3], v[7]);
+  cmp_swap(v[0], v[1]);
+  cmp_swap(v[2], v[3]);
+  cmp_swap(v[4], v[5]);
+  cmp_swap(v[6], v[7]);
+  cmp_swap(v[2], v[4]);
+  cmp_swap(v[3], v[5]);
+  cmp_swap(v[1], v[4]);
+  cmp_swap(v[3], v[6]);
+  cmp_swap(v[1], v[2]);
+  cmp_swap(v[3], v[4]);
+  cmp_swap(v[5], v[6]);
+}
+
+
+// Sort key of neighbour offset (dx, dy) with d2 = dx^2 + dy^2 <= 256^2 (the
+// wavefront offset radius): the sorted offset list's order -- ascending d2,
+// ties by descending position in the offset box, i.e. larger dy first, then
+// larger dx -- packed as d2 (17 bits), 256 - dy (9 bits), dx < 0 (1 bit).
+// On one circle and row the two points differ in the sign of dx, so the key
+// decodes back to (dx, dy).
+__device__ __forceinline__ uint32_t offset_key(int dx, int dy, int d2) {
+  return ((uint32_t)d2 << 11) | ((uint32_t)(256 - dy) << 1) | (dx < 0 ? 1u : 0u);
+}
+__device__ __forceinline__ int2 key_offset(uint32_t key) {
+  const int d2 = (int)(key >> 11), dy = 256 - (int)((key >> 1) & 0x3FFu), a2 = d2 - dy * dy;
+  int a = (int)sqrtf((float)a2);   // a2 <= 2^16 converts exactly; the root is corrected to the integer one
+  if (a * a > a2) a--;
+  else if ((a + 1) * (a + 1) <= a2) a++;
+  return make_int2((key & 1u) ? -a : a, dy);
 }
 
 // The patch from a finished register list: self, then the listed neighbours.
 __device__ int patch_from_topk(const Problem& pb, int px, int py, Patch& P, const WarpTopK& tk, int lane) {
-  const int bw = pb.boxW, bh = pb.boxH;
-  const unsigned W2 = 2u * bw - 1u;
   if (lane == 0) load_nb(pb, P, 0, 0, py * pb.tw + px);
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     const int i = 32 * h + lane;
     if (i < tk.cnt) {
-      const unsigned idx = 0xFFFFFFFFu - (unsigned)((h ? tk.hi : tk.lo) & 0xffffffffu);
-      const int dx = (int)(idx % W2) - (bw - 1), dy = (int)(idx / W2) - (bh - 1);
-      load_nb(pb, P, 1 + i, pack_off(dx, dy), (py + dy) * pb.tw + (px + dx));
+      const int2 o = key_offset(h ? tk.hi : tk.lo);
+      load_nb(pb, P, 1 + i, pack_off(o.x, o.y), (py + o.y) * pb.tw + (px + o.x));
     }
   }
   __syncwarp();
@@ -219,8 +263,8 @@ __device__ int patch_from_topk(const Problem& pb, int px, int py, Patch& P, cons
 }
 
 // Merges another warp's key list (ocnt keys in shared memory) into tk.
-__device__ void merge_keys(WarpTopK& tk, int lim, const unsigned long long* other, int ocnt, int lane) {
-  for (int base = 0; base < ocnt; base += 32) tk.insert(base + lane < ocnt ? other[base + lane] : ~0ull, lim, lane);
+__device__ void merge_keys(WarpTopK& tk, int lim, const uint32_t* other, int ocnt, int lane) {
+  for (int base = 0; base < ocnt; base += 32) tk.insert(base + lane < ocnt ? other[base + lane] : kNoKey, lim, lane);
 }
 
 // Patch neighbours when the valued pixels are exactly list[0 .. V) and nothing
@@ -234,20 +278,24 @@ __device__ void sparse_keys(const Problem& pb, int px, int py, WarpTopK& tk, con
   const int lim = pb.patchLimit - 1;
   const int bw = pb.boxW, bh = pb.boxH;
   for (int base = part * 32; base < V; base += 32 * parts * kU) {
-    unsigned long long key[kU];
+    uint32_t key[kU];
 #pragma unroll
     for (int u = 0; u < kU; u++) {
       const int j = base + 32 * parts * u + lane;
-      key[u] = ~0ull;
+      key[u] = kNoKey;
       if (j < V) {
         const int2 q = list[j];
         const int dx = q.x - px, dy = q.y - py;
         if (dx > -bw && dx < bw && dy > -bh && dy < bh) {
           const long long d2 = (long long)dx * dx + (long long)dy * dy;
-          if (d2 <= pb.maxD2) key[u] = offset_key(pb, dx, dy);
+          if (d2 <= pb.maxD2) key[u] = offset_key(dx, dy, (int)d2);
         }
       }
     }
+    // each lane's keys in ascending order: the first insertions fill the
+    // list with small keys, so later ones are mostly turned away by thr
+    static_assert(kU == 4, "four keys per lane");
+    sort4(key);
 #pragma unroll
     for (int u = 0; u < kU; u++) tk.insert(key[u], lim, lane);
   }
@@ -273,7 +321,7 @@ __device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int l
       // every pixel of ring R is at least (R - 1) * kCell + 1 away on one axis
       const long long dmin = (long long)(R - 1) * kCell + 1;
       if (dmin * dmin > pb.maxD2 || (dmin >= bw && dmin >= bh)) break;
-      if (tk.cnt == lim && (unsigned long long)(dmin * dmin) > (tk.thr >> 32)) break;
+      if (tk.cnt == lim && dmin * dmin > (long long)(tk.thr >> 11)) break;
     }
     const int ncell = R == 0 ? 1 : 8 * R;
     const int mine = ncell > part ? (ncell - part + parts - 1) / parts : 0;   // cells part, part + parts, ...
@@ -304,7 +352,7 @@ __device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int l
           const int ddx = max(0, max(x0 - px, px - (x0 + kCell - 1)));
           const int ddy = max(0, max(y0 - py, py - (y0 + kCell - 1)));
           const long long d2 = (long long)ddx * ddx + (long long)ddy * ddy;
-          want = d2 <= pb.maxD2 && ddx < bw && ddy < bh && (tk.cnt < lim || (unsigned long long)d2 <= (tk.thr >> 32));
+          want = d2 <= pb.maxD2 && ddx < bw && ddy < bh && (tk.cnt < lim || d2 <= (long long)(tk.thr >> 11));
         }
       }
       unsigned wm = __ballot_sync(kFull, want);
@@ -323,16 +371,18 @@ __device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int l
         }
         const int scx = __shfl_sync(kFull, qcx, src < 0 ? 0 : src), scy = __shfl_sync(kFull, qcy, src < 0 ? 0 : src);
         const int qy = (scy << kCellShift) + row, dy = qy - py;
-        unsigned long long key[kCell];
+        uint32_t key[kCell];
 #pragma unroll
         for (int j = 0; j < kCell; j++) {
           const int qx = (scx << kCellShift) + j, dx = qx - px;
-          key[j] = ~0ull;
+          key[j] = kNoKey;
           if (src >= 0 && qx < pb.tw && qy < pb.th && dx > -bw && dx < bw && dy > -bh && dy < bh) {
             const long long d2 = (long long)dx * dx + (long long)dy * dy;
-            if (d2 <= pb.maxD2 && pb.vis[qy * pb.tw + qx] < visCur) key[j] = offset_key(pb, dx, dy);
+            if (d2 <= pb.maxD2 && pb.vis[qy * pb.tw + qx] < visCur) key[j] = offset_key(dx, dy, (int)d2);
           }
         }
+        // each lane's row in ascending key order (see sparse_keys)
+        sort8(key);
 #pragma unroll
         for (int j = 0; j < kCell; j++) tk.insert(key[j], lim, lane);
       }
@@ -901,13 +951,13 @@ __device__ __forceinline__ unsigned wave_target(const WaveArgs& a, const Problem
     sparse_keys(pb, pos.x, pos.y, tk, a.targets, b0, lane, tw, G);
     if (G > 1) {
       // the other warps' lists go through their top-list areas
-      if (tw > 0) tk.store(reinterpret_cast<unsigned long long*>(T.region(warp) + sizeof(Patch)), lane);
+      if (tw > 0) tk.store(reinterpret_cast<uint32_t*>(T.region(warp) + sizeof(Patch)), lane);
       if (lane == 0) T.sGather[warp] = tk.cnt;
       T.sync();
       if (tw == 0)
         for (int w = 1; w < G; w++)
           merge_keys(tk, pb.patchLimit - 1,
-                     reinterpret_cast<const unsigned long long*>(T.region(lead + w) + sizeof(Patch)),
+                     reinterpret_cast<const uint32_t*>(T.region(lead + w) + sizeof(Patch)),
                      T.sGather[lead + w], lane);
     }
     if (tw == 0) nPatch = patch_from_topk(pb, pos.x, pos.y, P, tk, lane);
