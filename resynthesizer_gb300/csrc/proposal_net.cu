@@ -509,7 +509,9 @@ __global__ void k_gpack_t(const float* __restrict__ dy, int rows, int chunks, ui
   }
 }
 
-__global__ void k_bias_grad(const float* __restrict__ dy, int rows, float* __restrict__ gb) {
+// Per-block column sums of dY (part[block][32]); k_sum_parts adds the
+// blocks in order, so the bias gradient does not depend on block timing.
+__global__ void k_bias_grad(const float* __restrict__ dy, int rows, float* __restrict__ part) {
   __shared__ float red[8][32];
   const int c = threadIdx.x & 31, rl = threadIdx.x >> 5;
   float acc = 0.f;
@@ -519,7 +521,17 @@ __global__ void k_bias_grad(const float* __restrict__ dy, int rows, float* __res
   if (rl == 0) {
     float t = 0.f;
     for (int i = 0; i < 8; i++) t += red[i][c];
-    atomicAdd(gb + c, t);
+    part[(size_t)blockIdx.x * 32 + c] = t;
+  }
+}
+
+// out[i] = sum over z = 0 .. parts-1 of part[z * stride + i], in that order.
+__global__ void k_sum_parts(const float* __restrict__ part, int parts, long long stride, int n,
+                            float* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float t = 0.f;
+    for (int z = 0; z < parts; z++) t += part[z * stride + i];
+    out[i] = t;
   }
 }
 
@@ -547,12 +559,17 @@ __global__ void k_col2im(const float* __restrict__ dcol, int n, int l, const uin
   }
 }
 
-// grad[W_l[o][k]] = dWT_l[k][o]
-__global__ void k_gather_wgrad(const float* __restrict__ dwt, int l, float* __restrict__ grad) {
+// grad[W_l[o][k]] = dWT_l[k][o], summed over the K chunks' partial products
+// (chunk z at dwt + z * stride) in chunk order: the gradient is the same
+// every run.
+__global__ void k_gather_wgrad(const float* __restrict__ dwt, int chunks, long long stride, int l,
+                               float* __restrict__ grad) {
   const int K = k_of(l);
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < 32 * K; idx += gridDim.x * blockDim.x) {
     const int o = idx / K, k = idx - o * K;
-    grad[w_off(l) + idx] = dwt[(size_t)k * 32 + o];
+    float t = 0.f;
+    for (int z = 0; z < chunks; z++) t += dwt[z * stride + (size_t)k * 32 + o];
+    grad[w_off(l) + idx] = t;
   }
 }
 
@@ -632,6 +649,9 @@ __global__ void k_dump(Problem pb, const int2* __restrict__ targets, int npairs,
   }
 }
 
+// Blocks of the bias-gradient reduction (partial sums per block).
+constexpr int kBiasBlocks = 512;
+
 static int blocks_for(long long n, int threads, int cap = 4096) {
   return (int)std::max(1LL, std::min<long long>((n + threads - 1) / threads, cap));
 }
@@ -675,7 +695,8 @@ struct TResynthNet {
   uint16_t* g = nullptr;
   uint16_t* gT = nullptr;
   float* dcol = nullptr;
-  float* dwt[kLayers] = {};
+  float* dwt[kLayers] = {};    // per K chunk: partial dW^T of layer l
+  float* biasPart = nullptr;   // per block: partial bias gradients
   std::vector<void*> work;
   cudaStream_t stream = nullptr;
   std::mutex mu;
@@ -725,7 +746,7 @@ void ensure_work(TResynthNet* net, int n) {
     net->col[l] = walloc<uint16_t>(net, (size_t)tiles_rows(rows) * 128 * k_of(l));
     net->colT[l] = walloc<uint16_t>(net, (size_t)feat_tiles(l) * 128 * chunks_rows(rows) * 256);
     if (l < kLayers - 1) net->act[l] = walloc<uint16_t>(net, (size_t)rows * 32);
-    net->dwt[l] = walloc<float>(net, (size_t)feat_tiles(l) * 128 * 32);
+    net->dwt[l] = walloc<float>(net, (size_t)chunks_rows(rows) * feat_tiles(l) * 128 * 32);
   }
   // dY of layer l has rows_of(l) rows; dX of layer l's input has n * win^2 rows
   const size_t dyRows = std::max(maxRows, (size_t)n * 121);
@@ -735,6 +756,7 @@ void ensure_work(TResynthNet* net, int n) {
   net->g = walloc<uint16_t>(net, maxRows * 32);
   net->gT = walloc<uint16_t>(net, (size_t)32 * chunks_rows((int)maxRows) * 256);
   net->dcol = walloc<float>(net, maxRows * 288);
+  net->biasPart = walloc<float>(net, (size_t)kBiasBlocks * 32);
   net->cap = n;
 }
 
@@ -774,11 +796,12 @@ void train_backward(TResynthNet* net, int n, float* lossSlot, cudaStream_t s) {
     const float* dy = net->dy[cur];
     k_gpack<<<blocks_for((long long)tiles * 128 * 4, 256), 256, 0, s>>>(dy, rows, net->g);
     k_gpack_t<<<blocks_for(32LL * chunks * 32, 256), 256, 0, s>>>(dy, rows, chunks, net->gT);
-    k_bias_grad<<<blocks_for(rows, 8, 512), 256, 0, s>>>(dy, rows, net->grad + b_off(l));
+    const int bb = blocks_for(rows, 8, kBiasBlocks);
+    k_bias_grad<<<bb, 256, 0, s>>>(dy, rows, net->biasPart);
+    k_sum_parts<<<1, 32, 0, s>>>(net->biasPart, bb, 32, 32, net->grad + b_off(l));
     k_im2col_t<<<blocks_for((long long)feat_tiles(l) * 128 * chunks * 32, 256), 256, 0, s>>>(
         l == 0 ? net->x0 : net->act[l - 1], n, l, feat_tiles(l), chunks, net->colT[l]);
     NK(cudaGetLastError());
-    NK(cudaMemsetAsync(net->dwt[l], 0, (size_t)feat_tiles(l) * 128 * 32 * sizeof(float), s));
     tc::GemmArgs gw{};
     gw.A = net->colT[l];
     gw.B = net->gT;
@@ -788,12 +811,12 @@ void train_backward(TResynthNet* net, int n, float* lossSlot, cudaStream_t s) {
     gw.M = K;
     gw.N = 32;
     gw.K = 256;
-    gw.accumulate = 1;
     gw.outF = net->dwt[l];
+    gw.outChunk = (long long)feat_tiles(l) * 128 * 32;
     gw.ldo = 32;
     gw.err = net->err;
     NK(tc::launch_gemm(32, gw, feat_tiles(l), 1, chunks, s));
-    k_gather_wgrad<<<blocks_for(32LL * K, 256), 256, 0, s>>>(net->dwt[l], l, net->grad);
+    k_gather_wgrad<<<blocks_for(32LL * K, 256), 256, 0, s>>>(net->dwt[l], chunks, gw.outChunk, l, net->grad);
     NK(cudaGetLastError());
     if (l == 0) break;
     tc::GemmArgs gd{};

@@ -35,6 +35,7 @@ struct GemmArgs {
   int relu;
   int accumulate;            // atomicAdd the tile into outF (chunked K)
   float* outF;               // row-major, leading dimension ldo, or null
+  long long outChunk;        // chunked K without accumulate: chunk z writes outF + z * outChunk
   uint16_t* outH;            // bf16 bits, row-major, leading dimension ldo, or null
   int ldo;
   unsigned* err;             // bit 2: a wait ran out
@@ -185,6 +186,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (done) {
     const int row = blockIdx.x * kTileM + warp * 32 + lane;
+    float* outF = g.outF ? g.outF + blockIdx.z * g.outChunk : nullptr;
 #pragma unroll 1
     for (int c0 = 0; c0 < NT; c0 += 32) {
       uint32_t v[32];
@@ -198,12 +200,12 @@ __global__ void __launch_bounds__(128, 1) k_gemm(GemmArgs g) {
           float x = __uint_as_float(v[j]);
           const long long o = (long long)row * g.ldo + col;
           if (g.accumulate) {
-            atomicAdd(g.outF + o, x);
+            atomicAdd(outF + o, x);
             continue;
           }
           if (g.bias) x += g.bias[col];
           if (g.relu) x = fmaxf(x, 0.f);
-          if (g.outF) g.outF[o] = x;
+          if (outF) outF[o] = x;
           if (g.outH) g.outH[o] = __bfloat16_as_ushort(__float2bfloat16_rn(x));
         }
       }
