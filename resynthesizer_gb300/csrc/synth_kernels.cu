@@ -262,9 +262,15 @@ __device__ int patch_from_topk(const Problem& pb, int px, int py, Patch& P, cons
   return 1 + tk.cnt;
 }
 
-// Merges another warp's key list (ocnt keys in shared memory) into tk.
-__device__ void merge_keys(WarpTopK& tk, int lim, const uint32_t* other, int ocnt, int lane) {
-  for (int base = 0; base < ocnt; base += 32) tk.insert(base + lane < ocnt ? other[base + lane] : kNoKey, lim, lane);
+// Number of keys below k in the ascending list a[0 .. n).
+__device__ __forceinline__ int keys_below(const uint32_t* a, int n, uint32_t k) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (a[mid] < k) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
 }
 
 // Patch neighbours when the valued pixels are exactly list[0 .. V) and nothing
@@ -950,15 +956,35 @@ __device__ __forceinline__ unsigned wave_target(const WaveArgs& a, const Problem
     WarpTopK tk;
     sparse_keys(pb, pos.x, pos.y, tk, a.targets, b0, lane, tw, G);
     if (G > 1) {
-      // the other warps' lists go through their top-list areas
-      if (tw > 0) tk.store(reinterpret_cast<uint32_t*>(T.region(warp) + sizeof(Patch)), lane);
+      // Every warp's list goes to its top-list area.  A key's rank in the
+      // union is its index in its own list plus the keys below it in the
+      // others (keys are distinct, one per pixel); the keys of rank below
+      // lim land in the second warp's patch area (unused by the team).
+      const int lim = pb.patchLimit - 1;
+      auto list = [&](int w) { return reinterpret_cast<const uint32_t*>(T.region(lead + w) + sizeof(Patch)); };
+      uint32_t* merged = reinterpret_cast<uint32_t*>(T.region(lead + 1));
+      tk.store(reinterpret_cast<uint32_t*>(T.region(warp) + sizeof(Patch)), lane);
       if (lane == 0) T.sGather[warp] = tk.cnt;
       T.sync();
-      if (tw == 0)
-        for (int w = 1; w < G; w++)
-          merge_keys(tk, pb.patchLimit - 1,
-                     reinterpret_cast<const uint32_t*>(T.region(lead + w) + sizeof(Patch)),
-                     T.sGather[lead + w], lane);
+      int total = 0;
+      for (int w = 0; w < G; w++) total += T.sGather[lead + w];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int i = 32 * h + lane;
+        if (i < tk.cnt) {
+          const uint32_t k = h ? tk.hi : tk.lo;
+          int rank = i;
+          for (int w = 0; w < G; w++)
+            if (w != tw) rank += keys_below(list(w), T.sGather[lead + w], k);
+          if (rank < lim) merged[rank] = k;
+        }
+      }
+      T.sync();
+      if (tw == 0) {
+        tk.cnt = min(total, lim);
+        tk.lo = lane < tk.cnt ? merged[lane] : kNoKey;
+        tk.hi = 32 + lane < tk.cnt ? merged[32 + lane] : kNoKey;
+      }
     }
     if (tw == 0) nPatch = patch_from_topk(pb, pos.x, pos.y, P, tk, lane);
   } else if (tw == 0) {

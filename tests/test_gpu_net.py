@@ -128,6 +128,22 @@ def test_net_training_reduces_loss():
     pairs.close()
 
 
+def test_net_training_is_deterministic():
+    # the weight and bias gradients are summed in a fixed order (no float
+    # atomics): two networks trained alike end with identical parameters
+    n = 2048
+    x = _contexts(n, seed=9)
+    lab = np.random.default_rng(9).standard_normal((n, 2)).astype(np.float32)
+    pairs = R.Pairs(n)
+    assert pairs.add(x, lab) == n
+    a, b = R.Net(seed=13), R.Net(seed=13)
+    a.train(pairs, steps=40, batch=512, lr=1e-3)
+    b.train(pairs, steps=40, batch=512, lr=1e-3)
+    assert np.array_equal(a.get_params(), b.get_params())
+    for o in (a, b, pairs):
+        o.close()
+
+
 # ------------------------------------------------- the network in synthesis
 
 from resynthesizer_gb300 import workloads as W   # noqa: E402
