@@ -312,12 +312,8 @@ __device__ void sparse_keys(const Problem& pb, int px, int py, WarpTopK& tk, con
 // kCell cells in rings of growing distance, skipping cells where no pixel
 // has a value yet (least visit stamp) or that lie beyond the list's current
 // last entry.  Same neighbours as walking the offset list; cheap when the
-// nearest values are far away (deep inside a hole).  Part `part` of `parts`
-// warps owns the cells whose ring index is congruent to it; each part stops
-// on its own bound, and merging the parts' lists gives the lim smallest keys
-// (a key among the lim smallest overall is among the lim smallest of its part).
-__device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int lane, int visCur, int part,
-                          int parts) {
+// nearest values are far away (deep inside a hole).
+__device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int lane, int visCur) {
   const int lim = pb.patchLimit - 1;
   const int bw = pb.boxW, bh = pb.boxH;
   const int cx = px >> kCellShift, cy = py >> kCellShift;
@@ -330,12 +326,11 @@ __device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int l
       if (tk.cnt == lim && dmin * dmin > (long long)(tk.thr >> 11)) break;
     }
     const int ncell = R == 0 ? 1 : 8 * R;
-    const int mine = ncell > part ? (ncell - part + parts - 1) / parts : 0;   // cells part, part + parts, ...
-    for (int c0 = 0; c0 < mine; c0 += 32) {
-      const int ci = (c0 + lane) * parts + part;
+    for (int c0 = 0; c0 < ncell; c0 += 32) {
+      const int ci = c0 + lane;
       bool want = false;
       int qcx = cx, qcy = cy;
-      if (c0 + lane < mine) {
+      if (ci < ncell) {
         if (R > 0) {
           const int side = ci / (2 * R), o = ci - side * 2 * R;
           if (side == 0) {
@@ -399,7 +394,7 @@ __device__ void grid_keys(const Problem& pb, int px, int py, WarpTopK& tk, int l
 // One warp: the whole grid search.
 __device__ int build_patch_grid(const Problem& pb, int px, int py, Patch& P, int lane, int visCur) {
   WarpTopK tk;
-  grid_keys(pb, px, py, tk, lane, visCur, 0, 1);
+  grid_keys(pb, px, py, tk, lane, visCur);
   return patch_from_topk(pb, px, py, P, tk, lane);
 }
 
