@@ -527,29 +527,26 @@ __device__ void score_warp(const Problem& pb, const V& cv, const uint32_t* ct, c
           add += (i + u < n) ? v : 0u;
         }
       }
-      const int step = min(4, n - i);
       sum += add;
-      i += step;
-      terms += (unsigned)step;
+      i += min(4, n - i);
     }
+    // (sum, k) against the best (value, index) so far, as one 64-bit key
+    const unsigned long long mine = ((unsigned long long)sum << 32) | (unsigned)k;
     const bool done = active && i >= n;
-    const bool fin = done && (sum < bestVal || (sum == bestVal && k < bestIdx));
+    const bool fin = done && mine < (((unsigned long long)bestVal << 32) | (unsigned)bestIdx);
     if (__ballot_sync(kFull, fin)) {
-      unsigned long long key = fin ? ((unsigned long long)sum << 32) | (unsigned)k : ~0ull;
-      key = warp_min_u64(key);
-      const uint32_t kv = (uint32_t)(key >> 32);
-      const int ki = (int)(key & 0xffffffffu);
-      if (kv < bestVal || (kv == bestVal && ki < bestIdx)) {
-        bestVal = kv;
-        bestIdx = ki;
-      }
+      // every finished key is below the best, so their minimum replaces it
+      const unsigned long long key = warp_min_u64(fin ? mine : ~0ull);
+      bestVal = (uint32_t)(key >> 32);
+      bestIdx = (int)(key & 0xffffffffu);
     }
     // A lane stops when finished or when its partial sum can no longer win
     // (sums only grow; a tie wins only with the lower index).
-    const bool lost = active && !done && (sum > bestVal || (sum == bestVal && bestIdx < k));
+    const bool lost = active && !done && mine > (((unsigned long long)bestVal << 32) | (unsigned)bestIdx);
     const bool need = done || lost;
     const unsigned nm = __ballot_sync(kFull, need);
     if (need) {
+      terms += (unsigned)i;
       k = next + __popc(nm & lanemask_lt());
       // After a perfect match no later candidate can win.
       if (bestVal == 0u) k = INT_MAX;
