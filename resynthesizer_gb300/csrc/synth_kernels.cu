@@ -233,7 +233,7 @@ __device__ __forceinline__ void sort8(uint32_t* v) {
 // Sort key of neighbour offset (dx, dy) with d2 = dx^2 + dy^2 <= 256^2 (the
 // wavefront offset radius): the sorted offset list's order -- ascending d2,
 // ties by descending position in the offset box, i.e. larger dy first, then
-// larger dx -- packed as d2 (17 bits), 256 - dy (9 bits), dx < 0 (1 bit).
+// larger dx -- packed as d2 (17 bits), 256 - dy (10 bits: 0 .. 512), dx < 0 (1 bit).
 // On one circle and row the two points differ in the sign of dx, so the key
 // decodes back to (dx, dy).
 __device__ __forceinline__ uint32_t offset_key(int dx, int dy, int d2) {
