@@ -204,6 +204,21 @@ def test_wavefront_bit_exact_vs_wave_oracle(oracle, case):
     assert np.array_equal(r.out, out)
 
 
+@pytest.mark.parametrize("patch", [1, 2, 33, 64])
+@pytest.mark.parametrize("case", ["heal", "render"])
+def test_wavefront_patch_limits_vs_wave_oracle(oracle, case, patch):
+    """The pass-0 nearest-key lists at their limits -- one entry, 32 and 33
+    (both register halves), 63 -- on the cell-grid path (heal) and the
+    valued-list path with team merges (render) against the restatement."""
+    t, c, spec, kw = G.wave_small_case(case)
+    kw = dict(kw, patchSize=patch)
+    r = R.engine(t, c, R.format_indices(*spec), R.params(**kw), opts=R.options(mode=R.MODE_WAVEFRONT))
+    rc, out, passes, betters = oracle.wave_engine(make_params(**kw), oracle.format_indices(*spec), t, c)
+    assert r.rc == 0 == rc
+    assert r.stats["passes"] == passes and list(r.stats["betters"])[:passes] == betters
+    assert np.array_equal(r.out, out)
+
+
 @pytest.mark.parametrize("case", ["heal", "render", "mapstyle"])
 def test_wavefront_invariants_and_energy(oracle, case):
     if case == "heal":
@@ -265,7 +280,7 @@ def test_cell_grid_patches_equal_offset_walk(density):
     ys, xs = np.nonzero(hv == 0)
     pick = rng.choice(len(xs), 300, replace=False)
     targets = np.stack([xs[pick], ys[pick]], 1)
-    for p in (9, 16, 30, 64):
+    for p in (1, 2, 9, 16, 30, 33, 34, 64):   # list limits 1 .. 63, both register halves
         a = R.patch_neighbours(hv, p, targets, use_grid=False)
         b = R.patch_neighbours(hv, p, targets, use_grid=True)
         for i in range(len(targets)):
