@@ -1432,9 +1432,12 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi(const WaveArgs* jobs, int
 // A pass of many problems in one launch: steps 0 .. steps - 1, step b being
 // batch b of every request that has one.  prefix[b * (nreq + 1) + r] is the
 // first slot of request r in step b (prefix[... + nreq] = the step's total).
-// Work is handed out through a queue per step (queue[b], zeroed by the host):
-// a team takes the next slot as soon as it finishes one, so requests of
-// uneven cost share the GPU evenly.  A grid barrier closes each step (and,
+// Work per step: three quarters of the step's slots in fixed shares (a CTA's
+// teams on neighbouring slots, mostly of one request, whose patches and
+// shared probes meet in L1), then the rest through a queue per step
+// (queue[b], zeroed by the host): a team takes the next slot as soon as it
+// finishes one, so requests of uneven cost share the GPU evenly and the step
+// ends with its last target.  A grid barrier closes each step (and,
 // when some request stages its results, a commit phase between two
 // barriers).  Results equal one k_wave_multi (+ k_commit_multi) launch per
 // step.  Needs a cooperative launch.
@@ -1463,12 +1466,19 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi_persistent(const WaveArgs
     const WaveTeam T{G, team, warp % G, team * G, lane, warp, smem + WaveSmem::kHead, s_key, s_n, s_np, s_fast,
                      s_gather};
     const int visCur = pass == 0 ? b : 0x7ffffffe;
-    if (T.tw == 0 && lane == 0) s_item[team] = (int)atomicAdd(&queue[b], 1u);
-    T.sync();
-    int gs = s_item[team];
+    const int stride = gridDim.x * (wpb / G);
+    const int fixedEnd = (total * 3 / 4) / stride * stride;
+    int gs = blockIdx.x * (wpb / G) + team;
+    if (gs >= fixedEnd) {
+      if (T.tw == 0 && lane == 0) s_item[team] = fixedEnd + (int)atomicAdd(&queue[b], 1u);
+      T.sync();
+      gs = s_item[team];
+    }
     while (gs < total) {
+      const bool fixedNext = gs + stride < fixedEnd;
       int nxt = 0;
-      if (T.tw == 0 && lane == 0) nxt = (int)atomicAdd(&queue[b], 1u);   // in flight while this slot runs
+      if (!fixedNext && T.tw == 0 && lane == 0)
+        nxt = fixedEnd + (int)atomicAdd(&queue[b], 1u);   // in flight while this slot runs
       const int r = multi_request(sPrefix, nreq, gs);
       const WaveArgs& a = jobs[r];
       const Problem& pb = a.pb;
@@ -1483,6 +1493,10 @@ __global__ void __launch_bounds__(512, 2) k_wave_multi_persistent(const WaveArgs
       if (lane == 0) {
         atomicAdd(&a.ctr->terms, tv);
         atomicAdd(&a.ctr->evals, ev);
+      }
+      if (fixedNext) {
+        gs += stride;
+        continue;
       }
       if (T.tw == 0 && lane == 0) s_item[team] = nxt;
       T.sync();
