@@ -500,11 +500,13 @@ def spawn_pool(n: int):
 def cpu_reference_energies(name: str, mt_runs: int):
     """The single-threaded engine once, alone (its time is the CPU baseline),
     then `mt_runs` runs of the threaded engine (8 threads, nondeterministic)
-    side by side in spawned processes for their energies."""
+    in spawned processes, at most six side by side (more at once would load
+    the host cores more than the earlier lines did and shift the threaded
+    engine's interleaving), for their energies."""
     st_s, st_e, kind, st_out = cpu_engine(name, 1)
     mt = []
     if mt_runs:
-        with spawn_pool(mt_runs) as pool:
+        with spawn_pool(min(mt_runs, 6)) as pool:
             mt = pool.map(_cpu_job, [("engine", name, 8)] * mt_runs)
     return dict(st_seconds=st_s, st_energy=st_e, kind=kind, st_out=st_out,
                 mt_energies=[m[1] for m in mt], mt_seconds=[m[0] for m in mt])
@@ -518,6 +520,10 @@ def energy_vs_reference(e_gpu: float, ref: dict) -> dict:
          "cpu_mt_energies": mt, "cpu_mt_mean": mt_mean,
          "gpu_over_mt_mean": e_gpu / mt_mean if mt_mean else None,
          "mt_spread": (max(mt) - min(mt)) / mt_mean if mt_mean else None,
+         # the threaded engine is nondeterministic: the standard error of its
+         # mean, relative, says how far the gate's denominator moves run to run
+         "mt_mean_rel_stderr": float(np.std(mt, ddof=1) / np.sqrt(len(mt)) / mt_mean) if len(mt) > 1 else None,
+         "mt_seconds": ref.get("mt_seconds"),
          "mt_runs_at_or_above_gpu": sum(1 for m in mt if m >= e_gpu) if mt else None,
          "cpu_kind": ref["kind"],
          "gate": "wavefront energy at most 1.01 x the threaded reference's mean (one-sided: lower is better)"}
@@ -752,7 +758,7 @@ def main():
                     help="render1024 (default), heal256, heal4096, mapstyle2048, batchN")
     ap.add_argument("--quality", action="store_true", help="energy against the CPU engine instead of speed")
     ap.add_argument("--quality-runs", type=int, default=3)
-    ap.add_argument("--mt-runs", type=int, default=6, help="threaded CPU runs for the energy gate")
+    ap.add_argument("--mt-runs", type=int, default=12, help="threaded CPU runs for the energy gate")
     ap.add_argument("--concurrency", type=int, default=8, help="host workers for batch workloads")
     ap.add_argument("--learned", action="store_true", help="learned proposals against the plain search")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain object of the bench line")

@@ -1315,17 +1315,20 @@ __global__ void __launch_bounds__(512, 2) k_wave_persistent(WaveArgs a) {
       const WaveTeam T{G, team, warp % G, team * G, lane, warp, p, s_key, s_n, s_np, s_fast, s_gather};
       const bool sparse = a.sparse && (long long)b0 * b0 < a.sparseLimit2;
       const int visCur = a.pass == 0 ? b : 0x7ffffffe;
-      // Three quarters of the batch in fixed shares -- the teams of a CTA
-      // take neighbouring slots, whose patches overlap in L1 and, with probes
+      // Part of the batch in fixed shares -- the teams of a CTA take
+      // neighbouring slots, whose patches overlap in L1 and, with probes
       // shared by groups of 16 slots, whose probes read the same corpus
       // windows -- then the rest handed out one slot at a time from the
       // batch's queue, so that the batch ends when its last target does
-      // rather than when the team with the slowest share does (heal4096
-      // 22.8 -> 21.9 ms and mapstyle2048 95.0 -> 86.3 ms against fixed shares
-      // only; a half or an eighth in the queue did less).  One call site of
+      // rather than when the team with the slowest share does.  Measured
+      // (CUDA events): with shared probes three quarters fixed (heal4096
+      // 22.8 -> 21.9 ms, mapstyle2048 95.0 -> 86.3 ms against fixed shares
+      // only; half fixed 22.3 and 87.9 ms), with a staged corpus half fixed
+      // (render1024 9.29 -> 8.96 ms against three quarters; a quarter or
+      // three eighths the same, seven eighths 9.68 ms).  One call site of
       // wave_target: the kernel's code stays the size of one target's work.
       const int stride = gridDim.x * teamsPerBlock;
-      const int fixedEnd = a.queue ? (nslots * 3 / 4) / stride * stride : nslots;
+      const int fixedEnd = a.queue ? (a.probeShare ? nslots * 3 / 4 : nslots / 2) / stride * stride : nslots;
       int slot = blockIdx.x * teamsPerBlock + team;
       bool fixed = slot < fixedEnd;
       if (!fixed && fixedEnd < nslots) {
